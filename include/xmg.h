@@ -1,0 +1,108 @@
+/*
+ * libxm-gb300 extensions to the libxm C API.
+ *
+ * Everything declared in xm.h keeps the reference's behaviour (void return,
+ * fatal exit on error).  This header adds what a GB300 engine needs beyond
+ * that: status-code variants of the hot-path operations, the precision
+ * mode, per-call statistics and the hand-written contraction adjoint.
+ * Every function here is new; none replaces a reference symbol.
+ */
+#ifndef XMG_H_INCLUDED
+#define XMG_H_INCLUDED
+
+#include "tensor.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes returned by the xmg_* functions. */
+#define XMG_OK        0
+#define XMG_EINVAL    1   /* bad argument (indices, block structure, ...) */
+#define XMG_ENOMEM    2   /* host or device allocation failed             */
+#define XMG_ECUDA     3   /* CUDA runtime / kernel error                   */
+#define XMG_EIO       4   /* pagefile read/write failed                    */
+#define XMG_ETIMEOUT  5   /* a bounded device wait gave up                 */
+#define XMG_ENOTSUP   6   /* combination not supported                     */
+
+/* Message of the last failing xmg_* call on this thread. */
+const char *xmg_last_error(void);
+
+/* Precision of double / double complex contractions.
+ *   XMG_PREC_FP64  - plain FP64 grouped GEMM on the FP64 pipe.
+ *   XMG_PREC_EMU64 - split-precision emulated FP64: 6 signed 8-bit slices
+ *                    per operand as bf16 on tcgen05 tensor cores, exact
+ *                    FP32 partial sums drained into 64-bit integers, FP64
+ *                    only for scaling and the alpha*AB + beta*C fold.
+ *   XMG_PREC_AUTO  - EMU64 where it applies (power-of-two block-pair
+ *                    factors), FP64 elsewhere.  Default.
+ * float uses a compensated bf16 split in EMU modes and FP32 FMA in FP64
+ * mode; complex types decompose into real products.  The environment
+ * variable XMG_PRECISION=fp64|emu64|auto sets the initial mode. */
+#define XMG_PREC_FP64  0
+#define XMG_PREC_EMU64 1
+#define XMG_PREC_AUTO  2
+int xmg_set_precision(int mode);
+int xmg_get_precision(void);
+
+/* Status-code forms of the xm.h operations: same arguments and semantics,
+ * but errors return XMG_* instead of exiting. */
+int xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
+    xm_scalar_t beta, xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc);
+int xmg_add(xm_scalar_t alpha, xm_tensor_t *a, xm_scalar_t beta,
+    const xm_tensor_t *b, const char *idxa, const char *idxb);
+int xmg_set(xm_tensor_t *a, xm_scalar_t x);
+
+/* Useful (symmetry-reduced) flops of a contraction: 2*m*n*k summed over
+ * every canonical output block and surviving merged block pair, times 4
+ * for complex types.  Exactly the GEMM work the reference issues. */
+double xmg_contract_flops(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc);
+
+/* Merged block-pair structure of a contraction without running it:
+ * cb(cblock, re, im, m, n, k) once per surviving pair, cblock being the
+ * position in the canonical block list of c and (re, im) the pair factor
+ * s_a * s_b after merging.  Needs no device. */
+typedef void (*xmg_pair_cb)(size_t cblock, double re, double im, long m,
+    long n, long k);
+int xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, xmg_pair_cb cb);
+
+/* Statistics of the last xm_contract / xmg_contract on this process. */
+typedef struct {
+	double flops;            /* useful flops (see xmg_contract_flops) */
+	double ms_plan;          /* host planning, wall clock */
+	double ms_device;        /* device time of the contraction */
+	double ms_split;         /* of which: operand split / unfold kernels */
+	double ms_gemm;          /* of which: grouped GEMM kernel(s) */
+	long long n_cblocks;     /* canonical output blocks */
+	long long n_pairs;       /* merged block pairs issued */
+	long long slice_bytes;   /* bytes of staged operand slices */
+	int precision_used;      /* XMG_PREC_FP64 or XMG_PREC_EMU64 */
+	int gemm_launches;       /* kernels launched for the GEMM phase */
+} xmg_stats_t;
+int xmg_get_last_stats(xmg_stats_t *out);
+
+/* Hand-written adjoint of c = alpha * a * b over the index strings.  Given
+ * dc (same structure as c), accumulates into the canonical blocks of da
+ * and db (same structures as a and b):
+ *     da += d<L>/d(canonical a),  db += d<L>/d(canonical b)
+ * for L = sum over all blocks of dc o c (the xm_dot pairing), i.e. the
+ * contractions dc*b and a*dc projected onto canonical blocks with every
+ * derivative block's permutation and scalar folded back.  Either of da, db
+ * may be NULL.  Returns XMG_* status. */
+int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
+    const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,
+    xm_tensor_t *db, const char *idxa, const char *idxb, const char *idxc);
+
+/* Wait for all device work of the engine. */
+int xmg_synchronize(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* XMG_H_INCLUDED */

@@ -1,0 +1,89 @@
+"""Build libxm-gb300: C host sources + sm_103a CUDA kernels -> one shared
+library, libxm_gb300/lib/libxmgb.so, exporting the libxm C API (include/).
+
+Compiles in parallel, only what changed; no cmake.
+"""
+import concurrent.futures as cf
+import glob
+import os
+import platform
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build", platform.machine())
+LIB = os.path.join(HERE, "lib", "libxmgb.so")
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+INC = ["-I", os.path.join(ROOT, "include"), "-I", os.path.join(CSRC, "host"),
+       "-I", os.path.join(CSRC, "cuda")]
+CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-Wno-unused-parameter"]
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH
+
+
+def _headers():
+    return (glob.glob(os.path.join(ROOT, "include", "*.h")) +
+            glob.glob(os.path.join(CSRC, "*", "*.h")) +
+            glob.glob(os.path.join(CSRC, "*", "*.cuh")))
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src, verbose=False):
+    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    if not _stale(obj, [src] + _headers()):
+        return obj, None
+    if src.endswith(".cu"):
+        cmd = [NVCC] + NVFLAGS + INC + ["-c", src, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+    else:
+        cmd = ["gcc"] + CFLAGS + INC + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("compile failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return obj, (r.stdout + r.stderr).strip() or None
+
+
+def build(verbose=False):
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "host", "*.c")) +
+                  glob.glob(os.path.join(CSRC, "cuda", "*.cu")))
+    # the long CUDA translation units first
+    srcs.sort(key=lambda s: (not s.endswith(".cu"), s))
+    with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    objs = [o for o, _ in results]
+    for _, msg in results:
+        if msg and verbose:
+            print(msg)
+    if _stale(LIB, objs) or _arch_tag() != platform.machine():
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
+            "-lcudart_static", "-ldl", "-lrt", "-lpthread", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+        with open(LIB + ".arch", "w") as f:
+            f.write(platform.machine())
+    return LIB
+
+
+def _arch_tag():
+    try:
+        with open(LIB + ".arch") as f:
+            return f.read().strip()
+    except OSError:
+        return None
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,179 @@
+/*
+ * libxm-gb300 device runtime: one GPU, one engine stream, a stream-ordered
+ * HBM pool for block data, grow-only scratch and pinned staging buffers.
+ * All public copies are synchronous with respect to the calling host
+ * thread, matching the reference's synchronous API contract.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace xmg {
+
+static int g_ready = 0;
+static int g_dev = 0;
+static int g_sms = 0;
+static cudaStream_t g_stream = nullptr;
+static size_t g_in_use = 0;
+
+struct buf { void *p; size_t n; };
+static buf g_scratch[XMGD_SCRATCH_SLOTS];
+static buf g_pinned;
+
+cudaStream_t stream() { return g_stream; }
+int num_sms() { return g_sms; }
+
+int
+check(cudaError_t e, const char *what)
+{
+	if (e == cudaSuccess)
+		return XMG_OK;
+	cudaGetLastError();	/* clear the sticky-free error state */
+	if (e == cudaErrorMemoryAllocation)
+		return xmg_seterr(XMG_ENOMEM, "out of device memory (%s)", what);
+	return xmg_seterr(XMG_ECUDA, "CUDA error %s in %s",
+	    cudaGetErrorString(e), what);
+}
+
+} /* namespace xmg */
+
+using namespace xmg;
+
+extern "C" int
+xmgd_init(void)
+{
+	int n = 0;
+	cudaMemPool_t pool;
+	uint64_t thr = UINT64_MAX;
+
+	if (g_ready)
+		return XMG_OK;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+		cudaGetLastError();
+		return xmg_seterr(XMG_ECUDA, "no CUDA device available: the "
+		    "libxm-gb300 engine runs its kernels on the GPU only");
+	}
+	XMG_CK(cudaSetDevice(g_dev));
+	XMG_CK(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount,
+	    g_dev));
+	XMG_CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+	/* keep freed block memory in the pool: tensors are created and freed
+	 * often and cudaMalloc/cudaFree would synchronise the device */
+	XMG_CK(cudaDeviceGetDefaultMemPool(&pool, g_dev));
+	XMG_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold,
+	    &thr));
+	g_ready = 1;
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_alloc(size_t bytes, uint64_t *dptr)
+{
+	void *p = nullptr;
+
+	XMG_CK(cudaMallocAsync(&p, bytes, g_stream));
+	g_in_use += bytes;
+	*dptr = (uint64_t)(uintptr_t)p;
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_free(uint64_t dptr)
+{
+	XMG_CK(cudaFreeAsync((void *)(uintptr_t)dptr, g_stream));
+	return XMG_OK;
+}
+
+extern "C" size_t xmgd_arena_bytes_in_use(void) { return g_in_use; }
+
+extern "C" int
+xmgd_h2d(uint64_t dst, const void *src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst, src, bytes,
+	    cudaMemcpyHostToDevice, g_stream));
+	XMG_CK(cudaStreamSynchronize(g_stream));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_d2h(void *dst, uint64_t src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync(dst, (const void *)(uintptr_t)src, bytes,
+	    cudaMemcpyDeviceToHost, g_stream));
+	XMG_CK(cudaStreamSynchronize(g_stream));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_d2d(uint64_t dst, uint64_t src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst,
+	    (const void *)(uintptr_t)src, bytes, cudaMemcpyDeviceToDevice,
+	    g_stream));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_sync(void)
+{
+	if (!g_ready)
+		return XMG_OK;
+	XMG_CK(cudaStreamSynchronize(g_stream));
+	XMG_CK(cudaGetLastError());
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_is_device_ptr(const void *p)
+{
+	cudaPointerAttributes at;
+
+	if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	return at.type == cudaMemoryTypeDevice ||
+	    at.type == cudaMemoryTypeManaged;
+}
+
+extern "C" int
+xmgd_scratch(int slot, size_t bytes, uint64_t *dptr)
+{
+	buf *b;
+
+	if (slot < 0 || slot >= XMGD_SCRATCH_SLOTS)
+		return xmg_seterr(XMG_EINVAL, "bad scratch slot");
+	b = &g_scratch[slot];
+	if (b->n < bytes) {
+		if (b->p) {
+			XMG_CK(cudaStreamSynchronize(g_stream));
+			XMG_CK(cudaFree(b->p));
+			b->p = nullptr;
+			b->n = 0;
+		}
+		size_t n = bytes < 4096 ? 4096 : bytes + bytes / 4;
+		XMG_CK(cudaMalloc(&b->p, n));
+		b->n = n;
+	}
+	*dptr = (uint64_t)(uintptr_t)b->p;
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_pinned(size_t bytes, void **hptr)
+{
+	if (g_pinned.n < bytes) {
+		if (g_pinned.p) {
+			XMG_CK(cudaStreamSynchronize(g_stream));
+			XMG_CK(cudaFreeHost(g_pinned.p));
+			g_pinned.p = nullptr;
+			g_pinned.n = 0;
+		}
+		XMG_CK(cudaMallocHost(&g_pinned.p, bytes));
+		g_pinned.n = bytes;
+	}
+	*hptr = g_pinned.p;
+	return XMG_OK;
+}

@@ -1,0 +1,334 @@
+/*
+ * Block-data allocator for libxm-gb300.
+ *
+ * path == NULL: every allocation is a block of GPU memory from the engine's
+ * HBM arena and the handle is its device address.  This replaces the
+ * reference's malloc'd RAM storage (alloc.c:233-239); the handle stays an
+ * opaque "virtual pointer" and data moves through read/write with host
+ * buffers, exactly as the reference API promises (alloc.h:52-68).
+ *
+ * path != NULL: a pagefile of 512 KiB pages tracked by a first-fit bitmap
+ * that grows by doubling (by 256 GiB once past 256 GiB), handle = page
+ * offset | page count << 32, I/O in chunks of at most 1 GiB -- the
+ * reference's pagefile scheme (alloc.c:40-145, 249-300).  The contraction
+ * engine stages the pagefile blocks it touches into HBM (device views).
+ */
+#include <errno.h>
+#include <fcntl.h>
+#include <unistd.h>
+
+#include "xmg_host.h"
+#include "hmap.h"
+
+#define PAGE_BYTES (512ULL * 1024)
+#define GROW_STEP  (256ULL * 1024 * 1024 * 1024)
+#define IO_CHUNK   (1ULL << 30)
+
+struct xm_allocator {
+	char *path;
+	int fd;
+	uint64_t file_bytes;
+	unsigned char *used;      /* one bit per page */
+	xmg_hmap_t live;          /* HBM: live handle -> bytes */
+	xmg_hmap_t views;         /* pagefile: handle -> staged device addr */
+};
+
+static int bit_get(const unsigned char *b, uint64_t i) { return (b[i >> 3] >> (i & 7)) & 1; }
+static void bit_set(unsigned char *b, uint64_t i) { b[i >> 3] |= (unsigned char)(1u << (i & 7)); }
+static void bit_clr(unsigned char *b, uint64_t i) { b[i >> 3] &= (unsigned char)~(1u << (i & 7)); }
+
+int
+xmg_alloc_is_device(const xm_allocator_t *a)
+{
+	return a->path == NULL;
+}
+
+xm_allocator_t *
+xm_allocator_create(const char *path)
+{
+	xm_allocator_t *a;
+
+	if ((a = calloc(1, sizeof *a)) == NULL) {
+		perror("calloc");
+		return NULL;
+	}
+	xmg_hmap_init(&a->live);
+	xmg_hmap_init(&a->views);
+	a->fd = -1;
+	if (path == NULL) {
+		if (xmgd_init() != XMG_OK) {
+			fprintf(stderr, "libxm: %s\n", xmg_last_error());
+			free(a);
+			return NULL;
+		}
+		return a;
+	}
+	a->file_bytes = PAGE_BYTES;
+	if ((a->used = calloc(1, 1)) == NULL ||
+	    (a->path = strdup(path)) == NULL) {
+		perror("calloc");
+		free(a->used);
+		free(a);
+		return NULL;
+	}
+	if ((a->fd = open(path, O_CREAT | O_RDWR, 0600)) == -1) {
+		perror("open");
+		goto fail;
+	}
+	if (ftruncate(a->fd, (off_t)a->file_bytes)) {
+		perror("ftruncate");
+		close(a->fd);
+		goto fail;
+	}
+	return a;
+fail:
+	free(a->path);
+	free(a->used);
+	free(a);
+	return NULL;
+}
+
+const char *
+xm_allocator_get_path(xm_allocator_t *a)
+{
+	return a->path;
+}
+
+static int
+grow_file(xm_allocator_t *a)
+{
+	uint64_t oldmap, newmap, nb;
+	unsigned char *u;
+
+	oldmap = (a->file_bytes / PAGE_BYTES + 7) / 8;
+	nb = a->file_bytes > GROW_STEP ? a->file_bytes + GROW_STEP :
+	    2 * a->file_bytes;
+	newmap = (nb / PAGE_BYTES + 7) / 8;
+	if (ftruncate(a->fd, (off_t)nb)) {
+		perror("ftruncate");
+		return 1;
+	}
+	if ((u = realloc(a->used, newmap)) == NULL) {
+		perror("realloc");
+		return 1;
+	}
+	memset(u + oldmap, 0, newmap - oldmap);
+	a->used = u;
+	a->file_bytes = nb;
+	return 0;
+}
+
+/* First run of npages free pages starting at or after the first free page
+ * (alloc.c:104-128). */
+static uint64_t
+find_run(xm_allocator_t *a, uint64_t npages)
+{
+	uint64_t total = a->file_bytes / PAGE_BYTES, p, run = 0, s;
+
+	for (p = 0; p < total && bit_get(a->used, p); p++)
+		;
+	for (; p < total; p++) {
+		run = bit_get(a->used, p) ? 0 : run + 1;
+		if (run == npages) {
+			s = p + 1 - npages;
+			for (p = s; p < s + npages; p++)
+				bit_set(a->used, p);
+			return s | (npages << 32);
+		}
+	}
+	return XM_NULL_PTR;
+}
+
+uint64_t
+xm_allocator_allocate(xm_allocator_t *a, size_t bytes)
+{
+	uint64_t h, npages;
+
+	if (bytes == 0)
+		return XM_NULL_PTR;
+	if (a->path == NULL) {
+		if (xmgd_alloc(bytes, &h) != XMG_OK) {
+			fprintf(stderr, "libxm: %s\n", xmg_last_error());
+			return XM_NULL_PTR;
+		}
+		if (xmg_hmap_put(&a->live, h, bytes)) {
+			xmgd_free(h);
+			return XM_NULL_PTR;
+		}
+		return h;
+	}
+	npages = (bytes + PAGE_BYTES - 1) / PAGE_BYTES;
+	while ((h = find_run(a, npages)) == XM_NULL_PTR)
+		if (grow_file(a))
+			return XM_NULL_PTR;
+	return h;
+}
+
+static off_t
+page_offset(uint64_t h)
+{
+	return (off_t)((h & 0xffffffffULL) * PAGE_BYTES);
+}
+
+static int
+file_io(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes, int wr)
+{
+	off_t off = page_offset(h);
+	size_t n;
+	ssize_t r;
+
+	while (bytes > 0) {
+		n = bytes > IO_CHUNK ? IO_CHUNK : bytes;
+		r = wr ? pwrite(a->fd, mem, n, off) : pread(a->fd, mem, n, off);
+		if (r != (ssize_t)n)
+			return xmg_seterr(XMG_EIO, "%s", wr ? "pwrite" : "pread");
+		mem = (char *)mem + n;
+		off += (off_t)n;
+		bytes -= n;
+	}
+	return XMG_OK;
+}
+
+void
+xm_allocator_read(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes)
+{
+	if (h == XM_NULL_PTR)
+		xm_fatal("%s: data pointer is NULL", __func__);
+	if (a->path == NULL)
+		xmg_die_on(xmgd_d2h(mem, h, bytes));
+	else
+		xmg_die_on(file_io(a, h, mem, bytes, 0));
+}
+
+void
+xm_allocator_write(xm_allocator_t *a, uint64_t h, const void *mem, size_t bytes)
+{
+	if (h == XM_NULL_PTR)
+		xm_fatal("%s: data pointer is NULL", __func__);
+	if (a->path == NULL)
+		xmg_die_on(xmgd_h2d(h, mem, bytes));
+	else
+		xmg_die_on(file_io(a, h, (void *)mem, bytes, 1));
+}
+
+void
+xm_allocator_deallocate(xm_allocator_t *a, uint64_t h)
+{
+	uint64_t p, s, n;
+
+	if (h == XM_NULL_PTR)
+		return;
+	if (a->path == NULL) {
+		xmg_hmap_del(&a->live, h);
+		xmg_die_on(xmgd_free(h));
+		return;
+	}
+	s = h & 0xffffffffULL;
+	n = h >> 32;
+	for (p = s; p < s + n; p++)
+		bit_clr(a->used, p);
+}
+
+int
+xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
+    uint64_t *dptr)
+{
+	uint64_t d;
+	void *pin;
+	int st;
+
+	if (a->path == NULL) {
+		*dptr = h;
+		return XMG_OK;
+	}
+	if (xmg_hmap_get(&a->views, h, dptr))
+		return XMG_OK;
+	if ((st = xmgd_alloc(bytes, &d)) != XMG_OK)
+		return st;
+	if ((st = xmgd_pinned(bytes, &pin)) != XMG_OK ||
+	    (st = file_io(a, h, pin, bytes, 0)) != XMG_OK ||
+	    (st = xmgd_h2d(d, pin, bytes)) != XMG_OK) {
+		xmgd_free(d);
+		return st;
+	}
+	if (xmg_hmap_put(&a->views, h, d)) {
+		xmgd_free(d);
+		return xmg_seterr(XMG_ENOMEM, "out of memory");
+	}
+	*dptr = d;
+	return XMG_OK;
+}
+
+/* Write a staged view back to the pagefile. */
+int
+xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes)
+{
+	uint64_t d;
+	void *pin;
+	int st;
+
+	if (a->path == NULL)
+		return XMG_OK;
+	if (!xmg_hmap_get(&a->views, h, &d))
+		return xmg_seterr(XMG_EINVAL, "no staged view for handle");
+	if ((st = xmgd_pinned(bytes, &pin)) != XMG_OK ||
+	    (st = xmgd_d2h(pin, d, bytes)) != XMG_OK)
+		return st;
+	return file_io(a, h, pin, bytes, 1);
+}
+
+int
+xmg_alloc_release_views(xm_allocator_t *a, int write_back)
+{
+	size_t i;
+
+	(void)write_back;
+	if (a->path == NULL)
+		return XMG_OK;
+	for (i = 0; i < a->views.cap; i++)
+		if (a->views.keys[i] != XMG_HMAP_EMPTY)
+			xmgd_free(a->views.vals[i]);
+	xmg_hmap_free(&a->views);
+	xmg_hmap_init(&a->views);
+	return XMG_OK;
+}
+
+void
+xm_allocator_destroy(xm_allocator_t *a)
+{
+	size_t i;
+
+	if (a == NULL)
+		return;
+	if (a->path != NULL) {
+		xmg_alloc_release_views(a, 0);
+		if (close(a->fd))
+			perror("close");
+		if (unlink(a->path))
+			perror("unlink");
+	} else {
+		/* blocks still allocated when the allocator goes away */
+		for (i = 0; i < a->live.cap; i++)
+			if (a->live.keys[i] != XMG_HMAP_EMPTY)
+				xmgd_free(a->live.keys[i]);
+	}
+	xmg_hmap_free(&a->live);
+	xmg_hmap_free(&a->views);
+	free(a->path);
+	free(a->used);
+	free(a);
+}
+
+/* Read part of a block (byte range) into host memory; used by
+ * xm_tensor_get_element so that one element costs one small copy. */
+int
+xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
+    void *mem, size_t bytes)
+{
+	ssize_t r;
+
+	if (a->path == NULL)
+		return xmgd_d2h(mem, h + byte_off, bytes);
+	r = pread(a->fd, mem, bytes, page_offset(h) + (off_t)byte_off);
+	return r == (ssize_t)bytes ? XMG_OK : xmg_seterr(XMG_EIO, "pread");
+}

@@ -1,0 +1,615 @@
+/*
+ * Block-sparse contraction planner of libxm-gb300 (host, C).
+ *
+ * For every canonical block of c, in the canonical-list order, the planner
+ * enumerates the contraction block pairs, drops pairs with a zero block,
+ * forms alpha_pair = s_a * s_b, and merges pairs that read the same
+ * canonical data of a and b with the same permutation on the free indices
+ * by summing their factors in index order -- the reference's
+ * compute_block/same_contraction rules (contract.c:86-115, 161-192),
+ * restated with a hash on the pair key instead of the O(nblkk^2) scan so
+ * that production-size block grids plan in linear time.  Surviving pairs
+ * become one device plan: gather offset tables (the unfold/fold
+ * permutations, fused into the GEMM kernels), operand views for the split
+ * precision path and a work list for the grouped GEMM.
+ */
+#include <math.h>
+#include <time.h>
+
+#include "xmg_host.h"
+#include "hmap.h"
+
+static int g_precision = -1;
+static xmg_stats_t g_stats;
+
+static int
+precision_mode(void)
+{
+	const char *e;
+
+	if (g_precision < 0) {
+		g_precision = XMG_PREC_AUTO;
+		if ((e = getenv("XMG_PRECISION")) != NULL) {
+			if (strcmp(e, "fp64") == 0)
+				g_precision = XMG_PREC_FP64;
+			else if (strcmp(e, "emu64") == 0)
+				g_precision = XMG_PREC_EMU64;
+		}
+	}
+	return g_precision;
+}
+
+int
+xmg_set_precision(int mode)
+{
+	if (mode != XMG_PREC_FP64 && mode != XMG_PREC_EMU64 &&
+	    mode != XMG_PREC_AUTO)
+		return xmg_seterr(XMG_EINVAL, "xmg_set_precision: bad mode");
+	g_precision = mode;
+	return XMG_OK;
+}
+
+int xmg_get_precision(void) { return precision_mode(); }
+
+int
+xmg_get_last_stats(xmg_stats_t *out)
+{
+	*out = g_stats;
+	return XMG_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* offset-table pool with interning                                    */
+
+typedef struct {
+	int32_t *v;
+	int64_t n, cap;
+	xmg_hmap_t index;        /* descriptor hash -> offset */
+} tabpool_t;
+
+static int32_t
+tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
+{
+	uint64_t h = 0x9e3779b97f4a7c15ULL, off;
+	int64_t total = 1, e, r, o;
+	int d;
+
+	for (d = 0; d < nd; d++) {
+		h = xmg_hash64(h ^ (uint64_t)size[d] * 0x100000001b3ULL);
+		h = xmg_hash64(h ^ (uint64_t)stride[d]);
+		total *= size[d];
+	}
+	h = xmg_hash64(h ^ (uint64_t)nd);
+	if (h == XMG_HMAP_EMPTY)
+		h--;
+	if (xmg_hmap_get(&p->index, h, &off)) {
+		/* verify: recompute and compare (hash collisions are
+		 * astronomically rare, but never silently wrong) */
+		int same = 1;
+		for (e = 0; e < total && same; e++) {
+			r = e; o = 0;
+			for (d = 0; d < nd; d++) {
+				o += (r % size[d]) * stride[d];
+				r /= size[d];
+			}
+			same = off + (uint64_t)e < (uint64_t)p->n &&
+			    p->v[off + e] == (int32_t)o;
+		}
+		if (same)
+			return (int32_t)off;
+	}
+	while (p->n + total > p->cap) {
+		p->cap = p->cap ? 2 * p->cap : 4096;
+		if ((p->v = realloc(p->v, (size_t)p->cap * sizeof *p->v)) == NULL)
+			xm_fatal("%s: out of memory", __func__);
+	}
+	off = (uint64_t)p->n;
+	for (e = 0; e < total; e++) {
+		r = e; o = 0;
+		for (d = 0; d < nd; d++) {
+			o += (r % size[d]) * stride[d];
+			r /= size[d];
+		}
+		p->v[p->n++] = (int32_t)o;
+	}
+	xmg_hmap_put(&p->index, h, off);
+	return (int32_t)off;
+}
+
+/* Table over the masked dimensions of a block with the given strides. */
+static int32_t
+mask_table(tabpool_t *p, const xm_dim_t *dims, const int64_t *strides,
+    const xm_dim_t *mask)
+{
+	int64_t sz[XM_MAX_DIM], st[XM_MAX_DIM];
+	size_t k;
+
+	for (k = 0; k < mask->n; k++) {
+		sz[k] = (int64_t)dims->i[mask->i[k]];
+		st[k] = strides[mask->i[k]];
+	}
+	return tab_intern(p, (int)mask->n, sz, st);
+}
+
+/* ------------------------------------------------------------------ */
+/* the plan                                                            */
+
+typedef struct {
+	xm_scalar_type_t type;
+	xm_dim_t cidxa, aidxa, cidxb, aidxb, cidxc, aidxc;
+	/* growable arrays */
+	xmgd_cblock_t *cb; int ncb, capcb;
+	xmgd_pair_t *pr; int npr, cappr;
+	xmgd_view_t *va; int nva, capva;
+	xmgd_view_t *vb; int nvb, capvb;
+	xmg_hmap_t va_index, vb_index, ea_index, eb_index;
+	int32_t nexp_a, nexp_b;
+	tabpool_t tabs;
+	double flops;
+	uint8_t *emulatable;     /* per cblock */
+	int capem;
+} plan_t;
+
+#define GROW(arr, n, cap) do {						\
+	if ((n) == (cap)) {						\
+		(cap) = (cap) ? 2 * (cap) : 256;			\
+		if (((arr) = realloc((arr), (size_t)(cap) * sizeof *(arr))) == NULL) \
+			xm_fatal("%s: out of memory", __func__);	\
+	}								\
+} while (0)
+
+static void
+plan_free(plan_t *p)
+{
+	free(p->cb); free(p->pr); free(p->va); free(p->vb); free(p->tabs.v);
+	free(p->emulatable);
+	xmg_hmap_free(&p->tabs.index);
+	xmg_hmap_free(&p->va_index); xmg_hmap_free(&p->vb_index);
+	xmg_hmap_free(&p->ea_index); xmg_hmap_free(&p->eb_index);
+}
+
+/* Exponent-table slot for the free-block index of an operand block. */
+static int32_t
+exp_slot(xmg_hmap_t *index, int32_t *nexp, const xm_tensor_t *t,
+    xm_dim_t blk, const xm_dim_t *freemask, int32_t ncols)
+{
+	xm_dim_t nb = xm_block_space_get_nblocks(t->bs);
+	uint64_t key = 0, v;
+	size_t k;
+
+	for (k = 0; k < freemask->n; k++)
+		key = key * nb.i[freemask->i[k]] + blk.i[freemask->i[k]];
+	if (xmg_hmap_get(index, key, &v))
+		return (int32_t)v;
+	v = (uint64_t)*nexp;
+	*nexp += ncols;
+	xmg_hmap_put(index, key, v);
+	return (int32_t)v;
+}
+
+static int32_t
+view_id(xmgd_view_t **arr, int *n, int *cap, xmg_hmap_t *index,
+    uint64_t ptr, int32_t k, int32_t mn, int32_t rowtab, int32_t coltab,
+    int32_t exptab)
+{
+	uint64_t key = xmg_hash64(ptr ^ xmg_hash64(((uint64_t)(uint32_t)rowtab
+	    << 32) | (uint32_t)coltab)), v;
+	xmgd_view_t *w;
+	int i;
+
+	if (key == XMG_HMAP_EMPTY)
+		key--;
+	if (xmg_hmap_get(index, key, &v)) {
+		w = &(*arr)[v];
+		if (w->ptr == ptr && w->rowtab == rowtab && w->coltab == coltab)
+			return (int32_t)v;
+		for (i = 0; i < *n; i++) {	/* hash collision: scan */
+			w = &(*arr)[i];
+			if (w->ptr == ptr && w->rowtab == rowtab &&
+			    w->coltab == coltab)
+				return i;
+		}
+	}
+	GROW(*arr, *n, *cap);
+	w = &(*arr)[*n];
+	memset(w, 0, sizeof *w);
+	w->ptr = ptr; w->k = k; w->mn = mn;
+	w->rowtab = rowtab; w->coltab = coltab; w->exptab = exptab;
+	if (!xmg_hmap_get(index, key, NULL))
+		xmg_hmap_put(index, key, (uint64_t)*n);
+	return (*n)++;
+}
+
+/* +-2^t with |t| <= 16, real: the emulated path folds such factors into
+ * exact integer shifts. */
+static int
+pow2_factor(xm_scalar_t s, int *sign, int *shift)
+{
+	double r = creal(s), m;
+	int e;
+
+	if (cimag(s) != 0 || r == 0 || !isfinite(r))
+		return 0;
+	m = frexp(fabs(r), &e);
+	if (m != 0.5 || e - 1 < -16 || e - 1 > 16)
+		return 0;
+	*sign = r < 0 ? -1 : 1;
+	*shift = e - 1;
+	return 1;
+}
+
+struct cand {
+	xm_dim_t ia, ib;
+	xm_scalar_t al;
+	uint64_t da, db;
+};
+
+static int
+same_key(const xm_tensor_t *a, const xm_tensor_t *b, const struct cand *x,
+    const struct cand *y, const xm_dim_t *aidxa, const xm_dim_t *aidxb)
+{
+	struct xmg_block *pa = xmg_tensor_block(a, x->ia), *qa = xmg_tensor_block(a, y->ia);
+	struct xmg_block *pb = xmg_tensor_block(b, x->ib), *qb = xmg_tensor_block(b, y->ib);
+	size_t k;
+
+	if (x->da != y->da || x->db != y->db)
+		return 0;
+	for (k = 0; k < aidxa->n; k++)
+		if (pa->perm.i[aidxa->i[k]] != qa->perm.i[aidxa->i[k]])
+			return 0;
+	for (k = 0; k < aidxb->n; k++)
+		if (pb->perm.i[aidxb->i[k]] != qb->perm.i[aidxb->i[k]])
+			return 0;
+	return 1;
+}
+
+static uint64_t
+cand_hash(const xm_tensor_t *a, const xm_tensor_t *b, const struct cand *x,
+    const xm_dim_t *aidxa, const xm_dim_t *aidxb)
+{
+	struct xmg_block *pa = xmg_tensor_block(a, x->ia);
+	struct xmg_block *pb = xmg_tensor_block(b, x->ib);
+	uint64_t h = xmg_hash64(x->da) ^ (xmg_hash64(x->db) * 3);
+	size_t k;
+
+	for (k = 0; k < aidxa->n; k++)
+		h = xmg_hash64(h + pa->perm.i[aidxa->i[k]] + 1);
+	for (k = 0; k < aidxb->n; k++)
+		h = xmg_hash64(h + 31 * (pb->perm.i[aidxb->i[k]] + 1));
+	return h == XMG_HMAP_EMPTY ? h - 1 : h;
+}
+
+static double
+now_ms(void)
+{
+	struct timespec ts;
+
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+/* Validation and masks: contract.c:237-280, same messages. */
+static int
+check_contract(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, plan_t *p)
+{
+	const char *fn = "xm_contract";
+	size_t k;
+
+	if (a->allocator != c->allocator || b->allocator != c->allocator)
+		return xmg_seterr(XMG_EINVAL, "%s: tensors must use same "
+		    "allocator", fn);
+	if (a->type != c->type || b->type != c->type)
+		return xmg_seterr(XMG_EINVAL, "%s: tensors must have same "
+		    "scalar type", fn);
+	if (strlen(idxa) != xm_block_space_get_ndims(a->bs) ||
+	    strlen(idxb) != xm_block_space_get_ndims(b->bs) ||
+	    strlen(idxc) != xm_block_space_get_ndims(c->bs))
+		return xmg_seterr(XMG_EINVAL, "%s: bad contraction indices", fn);
+	xm_make_masks(idxa, idxb, &p->cidxa, &p->cidxb);
+	xm_make_masks(idxc, idxa, &p->cidxc, &p->aidxa);
+	xm_make_masks(idxc, idxb, &p->aidxc, &p->aidxb);
+	if (p->aidxa.n + p->cidxa.n != xm_block_space_get_ndims(a->bs) ||
+	    p->aidxb.n + p->cidxb.n != xm_block_space_get_ndims(b->bs) ||
+	    p->aidxc.n + p->cidxc.n != xm_block_space_get_ndims(c->bs))
+		return xmg_seterr(XMG_EINVAL, "%s: bad contraction indices", fn);
+	if (!(p->aidxc.n > 0 && p->aidxc.i[0] == 0) &&
+	    !(p->cidxc.n > 0 && p->cidxc.i[0] == 0))
+		return xmg_seterr(XMG_EINVAL, "%s: bad contraction indices", fn);
+	for (k = 0; k < p->cidxa.n; k++)
+		if (!xm_block_space_eq1(a->bs, p->cidxa.i[k], b->bs,
+		    p->cidxb.i[k]))
+			return xmg_seterr(XMG_EINVAL, "%s: inconsistent a and b "
+			    "tensor block-spaces", fn);
+	for (k = 0; k < p->cidxc.n; k++)
+		if (!xm_block_space_eq1(c->bs, p->cidxc.i[k], a->bs,
+		    p->aidxa.i[k]))
+			return xmg_seterr(XMG_EINVAL, "%s: inconsistent a and c "
+			    "tensor block-spaces", fn);
+	for (k = 0; k < p->aidxc.n; k++)
+		if (!xm_block_space_eq1(c->bs, p->aidxc.i[k], b->bs,
+		    p->aidxb.i[k]))
+			return xmg_seterr(XMG_EINVAL, "%s: inconsistent b and c "
+			    "tensor block-spaces", fn);
+	return XMG_OK;
+}
+
+/*
+ * Build the plan.  With device == 0 only the pair structure and flop count
+ * are computed (no data access).
+ */
+static int
+build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, plan_t *p, int device)
+{
+	xm_dim_t *list, nba, nbb, blkc, ia, ib, dims, dA, dB;
+	size_t nlist, nblkk, l, i;
+	struct cand *cand = NULL;
+	xmg_hmap_t merge;
+	int64_t sa[XM_MAX_DIM], sb[XM_MAX_DIM], sc[XM_MAX_DIM];
+	int32_t crow, ccol, arow, acol, brow, bcol, ea = 0, eb = 0;
+	struct xmg_block *ba, *bb;
+	uint64_t rep, dptr;
+	xmgd_cblock_t *cb;
+	xmgd_pair_t *pr;
+	int st = XMG_OK, sign, shift, emu;
+	double mult = xmg_is_complex(c->type) ? 8.0 : 2.0;
+
+	p->type = c->type;
+	nba = xm_block_space_get_nblocks(a->bs);
+	nbb = xm_block_space_get_nblocks(b->bs);
+	nblkk = xm_dim_dot_mask(&nba, &p->cidxa);
+	xm_tensor_get_canonical_block_list(c, &list, &nlist);
+	if (nblkk > 0 && (cand = malloc(nblkk * sizeof *cand)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	xmg_hmap_init(&merge);
+	for (l = 0; l < nlist && st == XMG_OK; l++) {
+		blkc = list[l];
+		dims = xm_block_space_get_block_dims(c->bs, blkc);
+		GROW(p->cb, p->ncb, p->capcb);
+		GROW(p->emulatable, p->ncb, p->capem);
+		cb = &p->cb[p->ncb];
+		memset(cb, 0, sizeof *cb);
+		cb->m = (int32_t)xm_dim_dot_mask(&dims, &p->cidxc);
+		cb->n = (int32_t)xm_dim_dot_mask(&dims, &p->aidxc);
+		cb->first_pair = p->npr;
+		emu = 1;
+		if (device) {
+			xmg_canon_strides(&dims, sc);
+			cb->crow = mask_table(&p->tabs, &dims, sc, &p->cidxc);
+			cb->ccol = mask_table(&p->tabs, &dims, sc, &p->aidxc);
+			if ((st = xmg_alloc_device_view(c->allocator,
+			    xm_tensor_get_block_data_ptr(c, blkc),
+			    xm_tensor_get_block_bytes(c, blkc), &dptr)) != XMG_OK)
+				break;
+			cb->c_ptr = dptr;
+		}
+		if (alpha == 0)	/* contract.c:159-160: no GEMMs */
+			goto next;
+		/* enumerate (contract.c:161-179) */
+		ia = xm_dim_zero(nba.n);
+		ib = xm_dim_zero(nbb.n);
+		xm_dim_set_mask(&ia, &p->aidxa, &blkc, &p->cidxc);
+		xm_dim_set_mask(&ib, &p->aidxb, &blkc, &p->aidxc);
+		for (i = 0; i < nblkk; i++) {
+			ba = xmg_tensor_block(a, ia);
+			bb = xmg_tensor_block(b, ib);
+			cand[i].ia = ia;
+			cand[i].ib = ib;
+			cand[i].al = 0;
+			if (ba->type != XM_BLOCK_TYPE_ZERO &&
+			    bb->type != XM_BLOCK_TYPE_ZERO) {
+				cand[i].al = xm_scalar_mul(ba->scalar,
+				    bb->scalar, c->type);
+				cand[i].da = xm_tensor_get_block_data_ptr(a, ia);
+				cand[i].db = xm_tensor_get_block_data_ptr(b, ib);
+			}
+			xm_dim_inc_mask(&ia, &nba, &p->cidxa);
+			xm_dim_inc_mask(&ib, &nbb, &p->cidxb);
+		}
+		/* merge (contract.c:180-192): first member of each class
+		 * accumulates the others' factors in index order */
+		xmg_hmap_free(&merge);
+		xmg_hmap_init(&merge);
+		for (i = 0; i < nblkk; i++) {
+			uint64_t h;
+			if (cand[i].al == 0)
+				continue;
+			h = cand_hash(a, b, &cand[i], &p->aidxa, &p->aidxb);
+			while (xmg_hmap_get(&merge, h, &rep) &&
+			    !same_key(a, b, &cand[rep], &cand[i], &p->aidxa,
+			    &p->aidxb))
+				h = xmg_hash64(h + 1);	/* collision: rehash */
+			if (xmg_hmap_get(&merge, h, &rep)) {
+				cand[rep].al = xm_scalar_add(cand[rep].al,
+				    cand[i].al, c->type);
+				cand[i].al = 0;
+			} else
+				xmg_hmap_put(&merge, h, i);
+		}
+		/* surviving pairs (contract.c:193-218) */
+		for (i = 0; i < nblkk; i++) {
+			if (cand[i].al == 0)
+				continue;
+			dA = xm_block_space_get_block_dims(a->bs, cand[i].ia);
+			dB = xm_block_space_get_block_dims(b->bs, cand[i].ib);
+			GROW(p->pr, p->npr, p->cappr);
+			pr = &p->pr[p->npr++];
+			memset(pr, 0, sizeof *pr);
+			pr->k = (int32_t)xm_dim_dot_mask(&dA, &p->cidxa);
+			xmg_scalar_pack(xm_scalar_mul(alpha, cand[i].al, c->type),
+			    pr->al);
+			p->flops += mult * cb->m * (double)cb->n * pr->k;
+			if (!pow2_factor(cand[i].al, &sign, &shift))
+				emu = 0;
+			if (!device)
+				continue;
+			xmg_tensor_block_strides(a, cand[i].ia, sa);
+			xmg_tensor_block_strides(b, cand[i].ib, sb);
+			arow = mask_table(&p->tabs, &dA, sa, &p->cidxa);
+			acol = mask_table(&p->tabs, &dA, sa, &p->aidxa);
+			brow = mask_table(&p->tabs, &dB, sb, &p->cidxb);
+			bcol = mask_table(&p->tabs, &dB, sb, &p->aidxb);
+			pr->arow = arow; pr->acol = acol;
+			pr->brow = brow; pr->bcol = bcol;
+			if ((st = xmg_alloc_device_view(a->allocator, cand[i].da,
+			    xm_tensor_get_block_bytes(a, cand[i].ia), &dptr)))
+				break;
+			pr->a_ptr = dptr;
+			if ((st = xmg_alloc_device_view(b->allocator, cand[i].db,
+			    xm_tensor_get_block_bytes(b, cand[i].ib), &dptr)))
+				break;
+			pr->b_ptr = dptr;
+			ea = exp_slot(&p->ea_index, &p->nexp_a, a, cand[i].ia,
+			    &p->aidxa, cb->m);
+			eb = exp_slot(&p->eb_index, &p->nexp_b, b, cand[i].ib,
+			    &p->aidxb, cb->n);
+			pr->aview = view_id(&p->va, &p->nva, &p->capva,
+			    &p->va_index, pr->a_ptr, pr->k, cb->m, arow, acol, ea);
+			pr->bview = view_id(&p->vb, &p->nvb, &p->capvb,
+			    &p->vb_index, pr->b_ptr, pr->k, cb->n, brow, bcol, eb);
+			cb->eA = ea;
+			cb->eB = eb;
+		}
+next:
+		cb->npairs = p->npr - cb->first_pair;
+		p->emulatable[p->ncb] = (uint8_t)emu;
+		p->ncb++;
+	}
+	xmg_hmap_free(&merge);
+	free(cand);
+	free(list);
+	return st;
+}
+
+static void
+init_plan(plan_t *p)
+{
+	memset(p, 0, sizeof *p);
+	xmg_hmap_init(&p->tabs.index);
+	xmg_hmap_init(&p->va_index);
+	xmg_hmap_init(&p->vb_index);
+	xmg_hmap_init(&p->ea_index);
+	xmg_hmap_init(&p->eb_index);
+}
+
+double
+xmg_contract_flops(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc)
+{
+	plan_t p;
+	double f = -1;
+
+	init_plan(&p);
+	if (check_contract(a, b, c, idxa, idxb, idxc, &p) == XMG_OK &&
+	    build_plan(1, a, b, c, &p, 0) == XMG_OK)
+		f = p.flops;
+	plan_free(&p);
+	return f;
+}
+
+int
+xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, xmg_pair_cb cb)
+{
+	plan_t p;
+	int st, l, q;
+
+	init_plan(&p);
+	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) == XMG_OK &&
+	    (st = build_plan(1, a, b, c, &p, 0)) == XMG_OK) {
+		for (l = 0; l < p.ncb; l++)
+			for (q = 0; q < p.cb[l].npairs; q++) {
+				const xmgd_pair_t *pr = &p.pr[p.cb[l].first_pair + q];
+				cb((size_t)l, pr->al[0], pr->al[1], p.cb[l].m,
+				    p.cb[l].n, pr->k);
+			}
+	}
+	plan_free(&p);
+	return st;
+}
+
+int
+xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
+    xm_scalar_t beta, xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc)
+{
+	xmgd_contract_t dp;
+	xmgd_timing_t tm;
+	plan_t p;
+	double t0 = now_ms();
+	int st, l;
+
+	init_plan(&p);
+	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) != XMG_OK)
+		goto out;
+	if ((st = xmgd_init()) != XMG_OK)
+		goto out;
+	if ((st = build_plan(alpha, a, b, c, &p, 1)) != XMG_OK)
+		goto out;
+	memset(&dp, 0, sizeof dp);
+	dp.dtype = c->type;
+	dp.precision = precision_mode();
+	xmg_scalar_pack(alpha, dp.alpha);
+	xmg_scalar_pack(beta, dp.beta);
+	dp.ncblocks = p.ncb;
+	dp.npairs = p.npr;
+	dp.cblocks = p.cb;
+	dp.pairs = p.pr;
+	dp.views_a = p.va;
+	dp.views_b = p.vb;
+	dp.nviews_a = p.nva;
+	dp.nviews_b = p.nvb;
+	dp.tabs = p.tabs.v;
+	dp.ntabs = p.tabs.n;
+	dp.nexp_a = p.nexp_a;
+	dp.nexp_b = p.nexp_b;
+	dp.flops = p.flops;
+	dp.emulatable = p.emulatable;
+	memset(&g_stats, 0, sizeof g_stats);
+	g_stats.ms_plan = now_ms() - t0;
+	st = xmgd_contract(&dp);
+	if (st == XMG_OK && !xmg_alloc_is_device(c->allocator)) {
+		for (l = 0; l < p.ncb && st == XMG_OK; l++) {
+			xm_dim_t *list; size_t n;
+			xm_tensor_get_canonical_block_list(c, &list, &n);
+			for (size_t q = 0; q < n && st == XMG_OK; q++)
+				st = xmg_alloc_commit_view(c->allocator,
+				    xm_tensor_get_block_data_ptr(c, list[q]),
+				    xm_tensor_get_block_bytes(c, list[q]));
+			free(list);
+			break;
+		}
+		xmg_alloc_release_views(c->allocator, 0);
+	}
+	xmgd_last_timing(&tm);
+	g_stats.flops = p.flops;
+	g_stats.ms_device = tm.ms_total;
+	g_stats.ms_split = tm.ms_split;
+	g_stats.ms_gemm = tm.ms_gemm;
+	g_stats.n_cblocks = p.ncb;
+	g_stats.n_pairs = p.npr;
+	g_stats.slice_bytes = tm.slice_bytes;
+	g_stats.precision_used = dp.precision_used;
+	g_stats.gemm_launches = tm.gemm_launches;
+out:
+	plan_free(&p);
+	return st;
+}
+
+void
+xm_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
+    xm_scalar_t beta, xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc)
+{
+	xmg_die_on(xmg_contract(alpha, a, b, beta, c, idxa, idxb, idxc));
+}
+
+int
+xmg_synchronize(void)
+{
+	return xmgd_sync();
+}

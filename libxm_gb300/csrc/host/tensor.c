@@ -1,0 +1,457 @@
+/*
+ * Block tensors for libxm-gb300.
+ *
+ * The block table mirrors the reference's struct xm_block
+ * (tensor.c:26-39): zero blocks carry nothing, canonical blocks an
+ * allocator handle, derivative blocks a permutation, a scalar and the
+ * linear index of their canonical source.  All validation rules and the
+ * index-0-fastest canonical block order are kept so that block lists,
+ * canonical mapping and sparsity are identical to the reference's.
+ *
+ * Block data lives in HBM (or a pagefile); unfold/fold run as CUDA kernels.
+ */
+#include "xmg_host.h"
+
+size_t
+xmg_tensor_block_linear(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	xm_dim_t nb = xm_block_space_get_nblocks(t->bs);
+
+	if (blkidx.n != nb.n || !xm_dim_less(&blkidx, &nb))
+		xm_fatal("%s: block index out of range", __func__);
+	return xm_dim_offset(&blkidx, &nb);
+}
+
+struct xmg_block *
+xmg_tensor_block(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return &t->blocks[xmg_tensor_block_linear(t, blkidx)];
+}
+
+void
+xmg_canon_strides(const xm_dim_t *dims, int64_t s[XM_MAX_DIM])
+{
+	size_t k;
+	int64_t acc = 1;
+
+	for (k = 0; k < dims->n; k++) {
+		s[k] = acc;
+		acc *= (int64_t)dims->i[k];
+	}
+}
+
+void
+xmg_tensor_block_strides(const xm_tensor_t *t, xm_dim_t blkidx,
+    int64_t strides[XM_MAX_DIM])
+{
+	struct xmg_block *b = xmg_tensor_block(t, blkidx);
+	xm_dim_t dims, cdims;
+	int64_t cs[XM_MAX_DIM];
+	size_t k;
+
+	/* The source block's dims are this block's dims permuted
+	 * (tensor.c:300-304); element el of this block is element
+	 * permute(el, perm) of the source (tensor.c:167-171). */
+	dims = xm_block_space_get_block_dims(t->bs, blkidx);
+	cdims = xm_dim_permute(&dims, &b->perm);
+	xmg_canon_strides(&cdims, cs);
+	for (k = 0; k < dims.n; k++)
+		strides[k] = cs[b->perm.i[k]];
+}
+
+xm_tensor_t *
+xm_tensor_create(const xm_block_space_t *bs, xm_scalar_type_t type,
+    xm_allocator_t *allocator)
+{
+	xm_tensor_t *t;
+	xm_dim_t nb;
+	size_t i;
+
+	if (bs == NULL || allocator == NULL)
+		xm_fatal("%s: invalid argument", __func__);
+	if (!xm_scalar_check_type(type))
+		xm_fatal("%s: unexpected scalar type", __func__);
+	if ((t = calloc(1, sizeof *t)) == NULL ||
+	    (t->bs = xm_block_space_clone(bs)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	t->type = type;
+	t->allocator = allocator;
+	nb = xm_block_space_get_nblocks(bs);
+	t->nblocks_total = xm_dim_dot(&nb);
+	if ((t->blocks = calloc(t->nblocks_total, sizeof *t->blocks)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < t->nblocks_total; i++) {
+		t->blocks[i].type = XM_BLOCK_TYPE_ZERO;
+		t->blocks[i].perm = xm_dim_identity_permutation(nb.n);
+		t->blocks[i].scalar = 0;
+		t->blocks[i].data = XM_NULL_PTR;
+	}
+	return t;
+}
+
+xm_tensor_t *
+xm_tensor_create_canonical(const xm_block_space_t *bs, xm_scalar_type_t type,
+    xm_allocator_t *allocator)
+{
+	xm_tensor_t *t = xm_tensor_create(bs, type, allocator);
+	xm_dim_t nb = xm_block_space_get_nblocks(bs), idx = xm_dim_zero(nb.n);
+
+	for (; xm_dim_ne(&idx, &nb); xm_dim_inc(&idx, &nb))
+		xm_tensor_set_canonical_block(t, idx);
+	return t;
+}
+
+xm_tensor_t *
+xm_tensor_create_structure(const xm_tensor_t *src, xm_scalar_type_t type,
+    xm_allocator_t *allocator)
+{
+	xm_tensor_t *t;
+	xm_dim_t nb, idx;
+	size_t i;
+
+	t = xm_tensor_create(src->bs, type,
+	    allocator ? allocator : src->allocator);
+	nb = xm_block_space_get_nblocks(src->bs);
+	idx = xm_dim_zero(nb.n);
+	for (i = 0; i < t->nblocks_total; i++, xm_dim_inc(&idx, &nb)) {
+		t->blocks[i] = src->blocks[i];
+		if (t->blocks[i].type == XM_BLOCK_TYPE_CANONICAL) {
+			t->blocks[i].type = XM_BLOCK_TYPE_ZERO;
+			xm_tensor_set_canonical_block(t, idx);
+		}
+	}
+	return t;
+}
+
+const xm_block_space_t *xm_tensor_get_block_space(const xm_tensor_t *t) { return t->bs; }
+xm_scalar_type_t xm_tensor_get_scalar_type(const xm_tensor_t *t) { return t->type; }
+xm_allocator_t *xm_tensor_get_allocator(const xm_tensor_t *t) { return t->allocator; }
+xm_dim_t xm_tensor_get_abs_dims(const xm_tensor_t *t) { return xm_block_space_get_abs_dims(t->bs); }
+xm_dim_t xm_tensor_get_nblocks(const xm_tensor_t *t) { return xm_block_space_get_nblocks(t->bs); }
+
+xm_block_type_t
+xm_tensor_get_block_type(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xmg_tensor_block(t, blkidx)->type;
+}
+
+xm_dim_t
+xm_tensor_get_block_dims(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xm_block_space_get_block_dims(t->bs, blkidx);
+}
+
+size_t
+xm_tensor_get_block_size(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xm_block_space_get_block_size(t->bs, blkidx);
+}
+
+size_t
+xm_tensor_get_block_bytes(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xm_tensor_get_block_size(t, blkidx) * xm_scalar_sizeof(t->type);
+}
+
+size_t
+xm_tensor_get_largest_block_size(const xm_tensor_t *t)
+{
+	return xm_block_space_get_largest_block_size(t->bs);
+}
+
+size_t
+xm_tensor_get_largest_block_bytes(const xm_tensor_t *t)
+{
+	return xm_tensor_get_largest_block_size(t) * xm_scalar_sizeof(t->type);
+}
+
+uint64_t
+xm_tensor_get_block_data_ptr(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	struct xmg_block *b = xmg_tensor_block(t, blkidx);
+
+	if (b->type == XM_BLOCK_TYPE_CANONICAL)
+		return b->data;
+	if (b->type == XM_BLOCK_TYPE_DERIVATIVE)
+		return t->blocks[b->data].data;
+	return XM_NULL_PTR;
+}
+
+xm_dim_t
+xm_tensor_get_block_permutation(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xmg_tensor_block(t, blkidx)->perm;
+}
+
+xm_scalar_t
+xm_tensor_get_block_scalar(const xm_tensor_t *t, xm_dim_t blkidx)
+{
+	return xmg_tensor_block(t, blkidx)->scalar;
+}
+
+xm_scalar_t
+xm_tensor_get_element(const xm_tensor_t *t, xm_dim_t idx)
+{
+	xm_dim_t blkidx, elidx;
+	struct xmg_block *b;
+	int64_t st[XM_MAX_DIM], off = 0;
+	size_t k, esz = xm_scalar_sizeof(t->type);
+	double buf[2] = {0, 0};
+	xm_scalar_t v;
+
+	xm_block_space_decompose_index(t->bs, idx, &blkidx, &elidx);
+	b = xmg_tensor_block(t, blkidx);
+	if (b->type == XM_BLOCK_TYPE_ZERO)
+		return 0;
+	xmg_tensor_block_strides(t, blkidx, st);
+	for (k = 0; k < elidx.n; k++)
+		off += (int64_t)elidx.i[k] * st[k];
+	xmg_die_on(xmg_alloc_read_range(t->allocator,
+	    xm_tensor_get_block_data_ptr(t, blkidx), (size_t)off * esz,
+	    buf, esz));
+	v = xm_scalar_get_element(buf, 0, t->type);
+	return xm_scalar_mul(b->scalar, v, t->type);
+}
+
+void
+xm_tensor_set_zero_block(xm_tensor_t *t, xm_dim_t blkidx)
+{
+	struct xmg_block *b = xmg_tensor_block(t, blkidx);
+
+	b->type = XM_BLOCK_TYPE_ZERO;
+	b->perm = xm_dim_identity_permutation(blkidx.n);
+	b->scalar = 0;
+	b->data = XM_NULL_PTR;
+}
+
+void
+xm_tensor_set_canonical_block(xm_tensor_t *t, xm_dim_t blkidx)
+{
+	uint64_t h;
+
+	if (xm_tensor_get_block_type(t, blkidx) != XM_BLOCK_TYPE_ZERO)
+		xm_fatal("%s: block must be zero", __func__);
+	h = xm_allocator_allocate(t->allocator,
+	    xm_tensor_get_block_bytes(t, blkidx));
+	if (h == XM_NULL_PTR)
+		xm_fatal("%s: unable to allocate block data", __func__);
+	xm_tensor_set_canonical_block_raw(t, blkidx, h);
+}
+
+void
+xm_tensor_set_canonical_block_raw(xm_tensor_t *t, xm_dim_t blkidx,
+    uint64_t data_ptr)
+{
+	struct xmg_block *b;
+
+	if (data_ptr == XM_NULL_PTR)
+		xm_fatal("%s: unexpected null data pointer", __func__);
+	if (xm_tensor_get_block_type(t, blkidx) != XM_BLOCK_TYPE_ZERO)
+		xm_fatal("%s: block must be zero", __func__);
+	b = xmg_tensor_block(t, blkidx);
+	b->type = XM_BLOCK_TYPE_CANONICAL;
+	b->perm = xm_dim_identity_permutation(blkidx.n);
+	b->scalar = 1;
+	b->data = data_ptr;
+}
+
+void
+xm_tensor_set_derivative_block(xm_tensor_t *t, xm_dim_t blkidx,
+    xm_dim_t source_blkidx, xm_dim_t permutation, xm_scalar_t scalar)
+{
+	struct xmg_block *b;
+	xm_dim_t d1, d2;
+
+	if (xm_tensor_get_block_type(t, blkidx) != XM_BLOCK_TYPE_ZERO)
+		xm_fatal("%s: block must be zero", __func__);
+	if (xm_tensor_get_block_type(t, source_blkidx) !=
+	    XM_BLOCK_TYPE_CANONICAL)
+		xm_fatal("%s: derivative blocks must have canonical source "
+		    "blocks", __func__);
+	d1 = xm_block_space_get_block_dims(t->bs, blkidx);
+	d1 = xm_dim_permute(&d1, &permutation);
+	d2 = xm_block_space_get_block_dims(t->bs, source_blkidx);
+	if (xm_dim_ne(&d1, &d2))
+		xm_fatal("%s: invalid block permutation", __func__);
+	b = xmg_tensor_block(t, blkidx);
+	b->type = XM_BLOCK_TYPE_DERIVATIVE;
+	b->perm = permutation;
+	b->scalar = scalar;
+	b->data = xmg_tensor_block_linear(t, source_blkidx);
+}
+
+void
+xm_tensor_get_canonical_block_list(const xm_tensor_t *t, xm_dim_t **blklist,
+    size_t *nblklist)
+{
+	xm_dim_t nb = xm_block_space_get_nblocks(t->bs), idx, *list = NULL;
+	size_t i, n = 0;
+
+	for (i = 0; i < t->nblocks_total; i++)
+		if (t->blocks[i].type == XM_BLOCK_TYPE_CANONICAL)
+			n++;
+	if (n > 0 && (list = malloc(n * sizeof *list)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	n = 0;
+	idx = xm_dim_zero(nb.n);
+	for (i = 0; i < t->nblocks_total; i++, xm_dim_inc(&idx, &nb))
+		if (t->blocks[i].type == XM_BLOCK_TYPE_CANONICAL)
+			list[n++] = idx;
+	*blklist = list;
+	*nblklist = n;
+}
+
+void
+xm_tensor_read_block(const xm_tensor_t *t, xm_dim_t blkidx, void *buf)
+{
+	if (xm_tensor_get_block_type(t, blkidx) == XM_BLOCK_TYPE_ZERO)
+		xm_fatal("%s: cannot read data from zero-blocks", __func__);
+	xm_allocator_read(t->allocator, xm_tensor_get_block_data_ptr(t, blkidx),
+	    buf, xm_tensor_get_block_bytes(t, blkidx));
+}
+
+void
+xm_tensor_write_block(xm_tensor_t *t, xm_dim_t blkidx, const void *buf)
+{
+	if (xm_tensor_get_block_type(t, blkidx) != XM_BLOCK_TYPE_CANONICAL)
+		xm_fatal("%s: can only write to canonical blocks", __func__);
+	xm_allocator_write(t->allocator, xm_tensor_get_block_data_ptr(t, blkidx),
+	    buf, xm_tensor_get_block_bytes(t, blkidx));
+}
+
+/*
+ * Iteration space of an unfold: mask_i positions (first fastest) then
+ * mask_j positions; matrix side offset i + stride * j; block side offset
+ * through the block's (permuted) strides.
+ */
+static void
+unfold_space(const xm_tensor_t *t, xm_dim_t blkidx, xm_dim_t mask_i,
+    xm_dim_t mask_j, size_t stride, int64_t *size, int64_t *mat_stride,
+    int64_t *blk_stride, int *ndim, size_t *span)
+{
+	xm_dim_t dims = xm_block_space_get_block_dims(t->bs, blkidx);
+	int64_t bs[XM_MAX_DIM], acc;
+	size_t k, ni, nj;
+	int n = 0;
+
+	xmg_tensor_block_strides(t, blkidx, bs);
+	acc = 1;
+	for (k = 0; k < mask_i.n; k++, n++) {
+		size[n] = (int64_t)dims.i[mask_i.i[k]];
+		mat_stride[n] = acc;
+		blk_stride[n] = bs[mask_i.i[k]];
+		acc *= size[n];
+	}
+	ni = (size_t)acc;
+	acc = (int64_t)stride;
+	nj = 1;
+	for (k = 0; k < mask_j.n; k++, n++) {
+		size[n] = (int64_t)dims.i[mask_j.i[k]];
+		mat_stride[n] = acc;
+		blk_stride[n] = bs[mask_j.i[k]];
+		acc *= size[n];
+		nj *= (size_t)size[n];
+	}
+	*ndim = n;
+	*span = (nj - 1) * stride + ni;	/* matrix elements touched */
+}
+
+/* Run one unfold (dir = 0) or fold (dir = 1) on the GPU.  Host buffers are
+ * staged through engine scratch; device buffers are used in place. */
+static void
+unfold_fold(const xm_tensor_t *t, xm_dim_t blkidx, xm_dim_t mask_i,
+    xm_dim_t mask_j, const void *from, void *to, size_t stride, int dir,
+    const char *fn)
+{
+	int64_t size[XM_MAX_DIM], ms[XM_MAX_DIM], bs[XM_MAX_DIM];
+	size_t span, blkbytes, esz = xm_scalar_sizeof(t->type), matbytes;
+	uint64_t dfrom, dto;
+	int ndim, dev_from, dev_to;
+	xmg_ptask_list_t l = {0};
+	xmgd_ptask_t *task;
+
+	if (from == NULL || to == NULL || from == to)
+		xm_fatal("%s: invalid argument", fn);
+	if (mask_i.n + mask_j.n != blkidx.n)
+		xm_fatal("%s: invalid mask dimensions", fn);
+	if (dir == 1 && xm_tensor_get_block_type(t, blkidx) !=
+	    XM_BLOCK_TYPE_CANONICAL)
+		xm_fatal("%s: can only fold canonical blocks", fn);
+	unfold_space(t, blkidx, mask_i, mask_j, stride, size, ms, bs, &ndim,
+	    &span);
+	blkbytes = xm_tensor_get_block_size(t, blkidx) * esz;
+	matbytes = span * esz;
+	xmg_die_on(xmgd_init());
+	dev_from = xmgd_is_device_ptr(from);
+	dev_to = xmgd_is_device_ptr(to);
+	if (dev_from)
+		dfrom = (uint64_t)(uintptr_t)from;
+	else {
+		xmg_die_on(xmgd_scratch(0, dir ? matbytes : blkbytes, &dfrom));
+		xmg_die_on(xmgd_h2d(dfrom, from, dir ? matbytes : blkbytes));
+	}
+	if (dev_to)
+		dto = (uint64_t)(uintptr_t)to;
+	else {
+		xmg_die_on(xmgd_scratch(1, dir ? blkbytes : matbytes, &dto));
+		/* elements of the destination outside the written pattern
+		 * must come back unchanged */
+		xmg_die_on(xmgd_h2d(dto, to, dir ? blkbytes : matbytes));
+	}
+	task = xmg_ptask_push(&l);
+	task->op = XMGD_OP_COPY;
+	task->alpha[0] = 1;
+	if (dir == 0) {		/* matrix <- block */
+		task->dst = dto;
+		task->src = dfrom;
+		xmg_ptask_shape(task, ndim, size, ms, bs);
+	} else {		/* block <- matrix */
+		task->dst = dto;
+		task->src = dfrom;
+		xmg_ptask_shape(task, ndim, size, bs, ms);
+	}
+	xmg_die_on(xmg_ptask_run(&l, t->type, t->type, NULL));
+	xmg_ptask_list_free(&l);
+	if (!dev_to)
+		xmg_die_on(xmgd_d2h(to, dto, dir ? blkbytes : matbytes));
+	xmg_die_on(xmgd_sync());
+}
+
+void
+xm_tensor_unfold_block(const xm_tensor_t *t, xm_dim_t blkidx, xm_dim_t mask_i,
+    xm_dim_t mask_j, const void *from, void *to, size_t stride)
+{
+	unfold_fold(t, blkidx, mask_i, mask_j, from, to, stride, 0, __func__);
+}
+
+void
+xm_tensor_fold_block(const xm_tensor_t *t, xm_dim_t blkidx, xm_dim_t mask_i,
+    xm_dim_t mask_j, const void *from, void *to, size_t stride)
+{
+	unfold_fold(t, blkidx, mask_i, mask_j, from, to, stride, 1, __func__);
+}
+
+void
+xm_tensor_free_block_data(xm_tensor_t *t)
+{
+	size_t i;
+
+	for (i = 0; i < t->nblocks_total; i++) {
+		if (t->blocks[i].type == XM_BLOCK_TYPE_CANONICAL)
+			xm_allocator_deallocate(t->allocator, t->blocks[i].data);
+		t->blocks[i].type = XM_BLOCK_TYPE_ZERO;
+		t->blocks[i].perm = xm_dim_identity_permutation(t->blocks[i].perm.n);
+		t->blocks[i].scalar = 0;
+		t->blocks[i].data = XM_NULL_PTR;
+	}
+}
+
+void
+xm_tensor_free(xm_tensor_t *t)
+{
+	if (t == NULL)
+		return;
+	xm_block_space_free(t->bs);
+	free(t->blocks);
+	free(t);
+}

@@ -1,0 +1,122 @@
+/*
+ * Interface between the libxm-gb300 C host layer and its CUDA kernels.
+ * Plain C types only; every function returns an XMG_* status code.
+ */
+#ifndef XMG_DEV_H
+#define XMG_DEV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- runtime: device, stream, HBM arena ---------------------------- */
+int xmgd_init(void);
+int xmgd_alloc(size_t bytes, uint64_t *dptr);
+int xmgd_free(uint64_t dptr);
+int xmgd_h2d(uint64_t dst, const void *src, size_t bytes);
+int xmgd_d2h(void *dst, uint64_t src, size_t bytes);
+int xmgd_d2d(uint64_t dst, uint64_t src, size_t bytes);
+int xmgd_sync(void);
+int xmgd_is_device_ptr(const void *p);
+/* Engine-owned grow-only device scratch, one buffer per slot. */
+#define XMGD_SCRATCH_SLOTS 16
+int xmgd_scratch(int slot, size_t bytes, uint64_t *dptr);
+/* Pinned host staging buffer (grow-only). */
+int xmgd_pinned(size_t bytes, void **hptr);
+size_t xmgd_arena_bytes_in_use(void);
+
+/* ---- permuted element-wise ops over blocks -------------------------- */
+enum {
+	XMGD_OP_SET = 0,    /* dst = alpha                               */
+	XMGD_OP_COPY,       /* dst = alpha * src   (with type conversion) */
+	XMGD_OP_SCALE,      /* dst = alpha * dst                          */
+	XMGD_OP_AXPY,       /* dst = alpha * dst + beta * src             */
+	XMGD_OP_MUL,        /* dst = (alpha * dst) * src                  */
+	XMGD_OP_DIV,        /* dst = dst / (alpha * src)                  */
+	XMGD_OP_DOT,        /* partial[task] += dst * src  (no store)     */
+};
+
+/* One block-sized task.  The iteration space has ndim dimensions of the
+ * given sizes; element (d_0..d_{n-1}) lives at dst + sum d_k*dst_stride[k]
+ * and src + sum d_k*src_stride[k] (strides in elements).  Dimension 0 must
+ * have dst_stride 1 for coalesced stores. */
+typedef struct {
+	uint64_t dst, src;
+	int32_t ndim, op;
+	int32_t size[8];
+	int64_t dst_stride[8], src_stride[8];
+	double alpha[2], beta[2];
+} xmgd_ptask_t;
+
+/* dtype/stype: xm_scalar_type_t values.  For XMGD_OP_DOT the per-task dot
+ * products (complex: re, im) are written to dots[2*ntasks] (host). */
+int xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
+    double *dots);
+
+/* ---- block-sparse contraction -------------------------------------- */
+
+/* One canonical output block.  Its m x n matrix view has element (i, j)
+ * at c_ptr + crow[i] + ccol[j]; i runs over the output dimensions shared
+ * with operand A, j over those shared with B. */
+typedef struct {
+	uint64_t c_ptr;
+	int32_t m, n;
+	int32_t crow, ccol;          /* offsets into the int32 table pool */
+	int32_t first_pair, npairs;
+	int32_t eA, eB;              /* exponent-table offsets (emulation) */
+} xmgd_cblock_t;
+
+/* One merged block pair: C += al * A^T B with A (k x m) and B (k x n),
+ * A(k, i) at a_ptr + arow[k] + acol[i] and likewise for B. */
+typedef struct {
+	uint64_t a_ptr, b_ptr;
+	int32_t k;
+	int32_t arow, acol, brow, bcol;
+	int32_t aview, bview;        /* operand-view ids (emulation) */
+	double al[2];
+} xmgd_pair_t;
+
+/* A distinct unfolded operand (block data + permutation + masks). */
+typedef struct {
+	uint64_t ptr;
+	int32_t k, mn;               /* rows (contracted), cols (free) */
+	int32_t rowtab, coltab;      /* table-pool offsets */
+	int32_t exptab;              /* exponent-table offset (per column) */
+	int32_t pad;
+	uint64_t slices;             /* device address of the tiled slices */
+} xmgd_view_t;
+
+typedef struct {
+	int dtype;                   /* xm_scalar_type_t */
+	int precision;               /* XMG_PREC_* */
+	double alpha[2], beta[2];
+	int ncblocks, npairs, nviews_a, nviews_b;
+	const xmgd_cblock_t *cblocks;
+	const xmgd_pair_t *pairs;
+	xmgd_view_t *views_a, *views_b;
+	const int32_t *tabs;         /* offset-table pool */
+	int64_t ntabs;
+	int32_t nexp_a, nexp_b;      /* exponent-table sizes */
+	double flops;                /* useful flops (reference counting) */
+	const uint8_t *emulatable;   /* per cblock: every pair factor +-2^t */
+	int precision_used;          /* out: XMG_PREC_FP64 / XMG_PREC_EMU64 */
+} xmgd_contract_t;
+
+int xmgd_contract(xmgd_contract_t *plan);
+
+/* Timing of the last xmgd_contract, milliseconds (device events). */
+typedef struct {
+	double ms_total, ms_split, ms_gemm;
+	int64_t slice_bytes;
+	int32_t gemm_launches, gemm_items;
+} xmgd_timing_t;
+void xmgd_last_timing(xmgd_timing_t *t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XMG_DEV_H */

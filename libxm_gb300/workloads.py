@@ -1,0 +1,231 @@
+"""Seeded synthetic block-tensor workloads built through the libxm API.
+
+The five contraction workloads measured by this project (ladder, uneven
+Z2^3-sparse ladder, permuted ring term, ladder adjoint, out-of-core
+production ladder) are generated here, identically for every library that
+exports the libxm API.  Values are uniform in [-1, 1] from a splitmix64
+stream keyed by (tensor seed, linear block index); canonical blocks that
+map onto themselves under a symmetry are projected onto the symmetric
+subspace after generation (the "antisymmetrised diagonal blocks").
+"""
+import numpy as np
+
+from . import api
+
+GAMMA = np.uint64(0x9E3779B97F4A7C15)
+M1 = np.uint64(0xBF58476D1CE4E5B9)
+M2 = np.uint64(0x94D049BB133111EB)
+
+# symmetry groups as (permutation, factor); block index map b'[k] = b[perm[k]]
+LADDER_ANTISYM = [((0, 1, 2, 3), 1.0), ((1, 0, 2, 3), -1.0),
+                  ((0, 1, 3, 2), -1.0), ((1, 0, 3, 2), 1.0)]
+PAIR_SYM = [((0, 1, 2, 3), 1.0), ((2, 3, 0, 1), 1.0)]
+NO_SYM = [((0, 1, 2, 3), 1.0)]
+
+
+def splitmix64(seed, n):
+    """n consecutive splitmix64 outputs after state = seed."""
+    with np.errstate(over="ignore"):
+        x = np.uint64(seed) + GAMMA * np.arange(1, n + 1, dtype=np.uint64)
+        x = (x ^ (x >> np.uint64(30))) * M1
+        x = (x ^ (x >> np.uint64(27))) * M2
+        x = x ^ (x >> np.uint64(31))
+    return x
+
+
+def uniform(seed, n):
+    """n values uniform in [-1, 1) from the splitmix64 stream of seed."""
+    return (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * (2.0 ** -52) - 1.0
+
+
+def block_seed(tseed, lin):
+    return int(splitmix64((int(tseed) * 0x100000001B3 + int(lin)) & (2**64 - 1), 1)[0])
+
+
+def uneven_sizes(total, nblk, lo, hi, seed):
+    """Seeded block sizes in [lo, hi] summing to total."""
+    r = splitmix64(seed, 4 * nblk * nblk + 16)
+    sizes = [total // nblk] * nblk
+    for k in range(total - sum(sizes)):
+        sizes[k] += 1
+    p = 0
+    for _ in range(4 * nblk):
+        i = int(r[p] % nblk); j = int(r[p + 1] % nblk)
+        d = int(r[p + 2] % 9)
+        p += 3
+        if i == j:
+            continue
+        d = min(d, sizes[i] - lo, hi - sizes[j])
+        if d > 0:
+            sizes[i] -= d
+            sizes[j] += d
+    assert sum(sizes) == total and min(sizes) >= lo and max(sizes) <= hi
+    return sizes
+
+
+def labels(n, seed):
+    return [int(v % 8) for v in splitmix64(seed, n)]
+
+
+def make_space(lib, sizes_per_dim):
+    dims = [sum(s) for s in sizes_per_dim]
+    bs = api.BlockSpace(lib, dims)
+    for d, sizes in enumerate(sizes_per_dim):
+        x = 0
+        for s in sizes[:-1]:
+            x += s
+            bs.split(d, x)
+    return bs
+
+
+def symmetric_tensor(lib, alloc, bs, dtype, group, allowed=None):
+    """Canonical/derivative structure like the reference's test builders:
+    visit block indices with the last position fastest; an unassigned,
+    allowed block becomes canonical and its images under the group become
+    derivative blocks (when still unassigned)."""
+    t = api.Tensor(lib, bs, dtype, alloc)
+    nb = bs.nblocks()
+    for blk in np.ndindex(*nb):
+        if t.block_type(blk) != api.ZERO:
+            continue
+        if allowed is not None and not allowed(blk):
+            continue
+        t.set_canonical(blk)
+        for perm, s in group[1:]:
+            b2 = tuple(blk[perm[k]] for k in range(len(blk)))
+            if t.block_type(b2) == api.ZERO:
+                t.set_derivative(b2, blk, perm, s)
+    return t
+
+
+def fill(t, seed, group=NO_SYM):
+    """Write seeded uniform[-1,1] data into every canonical block; project
+    blocks that are their own image under the group."""
+    nb = t.nblocks()
+    cplx = t.dtype in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX)
+    for blk in t.canonical_blocks():
+        dims = t.block_dims(blk)
+        n = int(np.prod(dims))
+        lin = int(np.ravel_multi_index(blk, nb, order="F"))
+        s0 = block_seed(seed, lin)
+        v = uniform(s0, n)
+        if cplx:
+            v = v + 1j * uniform(s0 ^ 0x5555, n)
+        x = v.reshape(dims, order="F")
+        stab = [(p, s) for p, s in group
+                if tuple(blk[p[k]] for k in range(len(blk))) == tuple(blk)]
+        if len(stab) > 1:
+            x = sum(s * np.transpose(x, p) for p, s in stab) / len(stab)
+        t.write_block(blk, x)
+
+
+class Workload:
+    """Three tensors and a contraction c = alpha * a * b + beta * c."""
+
+    def __init__(self, name, a, b, c, idx, alpha, beta, groups, seeds, extra=None):
+        self.name = name
+        self.a, self.b, self.c = a, b, c
+        self.idxa, self.idxb, self.idxc = idx
+        self.alpha, self.beta = alpha, beta
+        self.groups = groups
+        self.seeds = seeds
+        self.extra = extra or {}
+
+    def tensors(self):
+        return [self.a, self.b, self.c]
+
+    def run(self):
+        api.contract(self.alpha, self.a, self.b, self.beta, self.c,
+                     self.idxa, self.idxb, self.idxc)
+
+    def free(self):
+        for t in self.tensors():
+            t.free()
+
+
+def ladder(lib, alloc, o_sizes, v_sizes, seed=1, dtype=api.DOUBLE, z2=None,
+           with_c_fill=False):
+    """C(i,j,a,b) = sum_{c,d} A(i,j,c,d) B(c,d,a,b) with i<->j, c<->d, a<->b
+    antisymmetry (factor -1 derivative blocks) and optional Z2^3 labels."""
+    bso = [o_sizes, o_sizes, v_sizes, v_sizes]
+    bsv = [v_sizes] * 4
+    sa, sb = make_space(lib, bso), make_space(lib, bsv)
+    alw_a = alw_b = None
+    if z2 is not None:
+        lo, lv = z2
+        alw_a = lambda b: (lo[b[0]] ^ lo[b[1]] ^ lv[b[2]] ^ lv[b[3]]) == 0
+        alw_b = lambda b: (lv[b[0]] ^ lv[b[1]] ^ lv[b[2]] ^ lv[b[3]]) == 0
+    a = symmetric_tensor(lib, alloc, sa, dtype, LADDER_ANTISYM, alw_a)
+    b = symmetric_tensor(lib, alloc, sb, dtype, LADDER_ANTISYM, alw_b)
+    c = symmetric_tensor(lib, alloc, sa, dtype, LADDER_ANTISYM, alw_a)
+    sa.free(); sb.free()
+    fill(a, seed * 3 + 1, LADDER_ANTISYM)
+    fill(b, seed * 3 + 2, LADDER_ANTISYM)
+    if with_c_fill:
+        fill(c, seed * 3 + 3, LADDER_ANTISYM)
+    return Workload("ladder", a, b, c, ("ijcd", "cdab", "ijab"), 1.0, 0.0,
+                    (LADDER_ANTISYM, LADDER_ANTISYM, LADDER_ANTISYM),
+                    (seed * 3 + 1, seed * 3 + 2, seed * 3 + 3))
+
+
+def cfg1(lib, alloc, seed=1):
+    """Plain FP64 ladder, CPU-runnable: o = 24 as 3 x 8, v = 64 as 4 x 16."""
+    w = ladder(lib, alloc, [8] * 3, [16] * 4, seed)
+    w.name = "cfg1_ladder_o24_v64"
+    return w
+
+
+def cfg2_shape(seed=2):
+    o = uneven_sizes(96, 6, 8, 24, seed * 7 + 11)
+    v = uneven_sizes(384, 12, 16, 48, seed * 7 + 12)
+    lo = labels(6, seed * 7 + 13)
+    lv = labels(12, seed * 7 + 14)
+    return o, v, lo, lv
+
+
+def cfg2(lib, alloc, seed=2, scale=1):
+    """Uneven-block Z2^3-sparse FP64 ladder: o = 96 in 6 blocks of 8..24,
+    v = 384 in 12 blocks of 16..48.  scale > 1 shrinks every block size by
+    that factor (structure preserved) for quick parity runs."""
+    o, v, lo, lv = cfg2_shape(seed)
+    if scale > 1:
+        o = [max(1, x // scale) for x in o]
+        v = [max(1, x // scale) for x in v]
+    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv))
+    w.name = "cfg2_ladder_o96_v384_z2" if scale == 1 else "cfg2_ladder_scaled_%d" % scale
+    w.extra = {"o_sizes": o, "v_sizes": v, "o_labels": lo, "v_labels": lv}
+    return w
+
+
+def cfg3(lib, alloc, dtype=api.FLOAT, seed=3, o_blk=16, v_blk=32, no=4, nv=8):
+    """Ring term C(i,a,j,b) += sum_{k,c} A(k,i,c,a) B(j,k,b,c), beta = 1,
+    C prefilled; (i,a) <-> (j,b) pair symmetry (+1) on C only, A and B
+    fully canonical."""
+    o, v = [o_blk] * no, [v_blk] * nv
+    sab = make_space(lib, [o, o, v, v])
+    sc = make_space(lib, [o, v, o, v])
+    a = api.Tensor(lib, sab, dtype, alloc, canonical=True)
+    b = api.Tensor(lib, sab, dtype, alloc, canonical=True)
+    c = symmetric_tensor(lib, alloc, sc, dtype, PAIR_SYM)
+    sab.free(); sc.free()
+    fill(a, seed * 3 + 1)
+    fill(b, seed * 3 + 2)
+    fill(c, seed * 3 + 3, PAIR_SYM)
+    return Workload("cfg3_ring_o64_v256", a, b, c, ("kica", "jkbc", "iajb"),
+                    1.0, 1.0, (NO_SYM, NO_SYM, PAIR_SYM),
+                    (seed * 3 + 1, seed * 3 + 2, seed * 3 + 3))
+
+
+def read_canonical(t):
+    """{block index: raw canonical data} of a tensor."""
+    return {blk: t.read_block(blk) for blk in t.canonical_blocks()}
+
+
+def rel_frobenius(x, ref):
+    """sqrt(sum |x - ref|^2) / sqrt(sum |ref|^2) over matching blocks."""
+    num = den = 0.0
+    for k, r in ref.items():
+        d = x[k].astype(np.complex128) - r.astype(np.complex128)
+        num += float(np.vdot(d, d).real)
+        den += float(np.vdot(r.astype(np.complex128), r.astype(np.complex128)).real)
+    return (num ** 0.5) / (den ** 0.5 if den > 0 else 1.0)

@@ -1,0 +1,84 @@
+"""Shared test helpers: seeded fills and case runners."""
+import ctypes as C
+
+import numpy as np
+
+from libxm_gb300 import api
+
+TOL = {api.FLOAT: 1e-4, api.FLOAT_COMPLEX: 1e-4, api.DOUBLE: 1e-8,
+       api.DOUBLE_COMPLEX: 1e-8}       # test.c:48-70 (absolute)
+TYPES = [api.FLOAT, api.FLOAT_COMPLEX, api.DOUBLE, api.DOUBLE_COMPLEX]
+TYPE_NAMES = {0: "float", 1: "cfloat", 2: "double", 3: "cdouble"}
+
+
+def fill_random(t, rng):
+    """drand48() - 0.5 style values (test.c:72-132), from a numpy stream."""
+    for blk in t.canonical_blocks():
+        n = t.block_size(blk)
+        v = rng.random(n) - 0.5
+        if t.dtype in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX):
+            v = v + 1j * (rng.random(n) - 0.5)
+        t.write_block(blk, v)
+
+
+def scalar(rng, dtype):
+    if dtype in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX):
+        return complex(rng.random() - 0.5, rng.random() - 0.5)
+    return rng.random() - 0.5
+
+
+def canon(t):
+    return {blk: t.read_block(blk) for blk in t.canonical_blocks()}
+
+
+def max_abs_diff(x, y):
+    assert x.keys() == y.keys()
+    m = 0.0
+    for k in x:
+        if x[k].size:
+            m = max(m, float(np.max(np.abs(x[k].astype(np.complex128) - y[k].astype(np.complex128)))))
+    return m
+
+
+def run_contract_case(lib, alloc, case, dtype, seed, alpha, beta, pagefile=None):
+    """Build a reference test case on lib, fill it from seed, contract.
+    Returns (outputs of c's canonical blocks, tensors)."""
+    make, ia, ib, ic = case
+    a, b, c = make(lib, alloc, dtype)
+    rng = np.random.default_rng(seed)
+    fill_random(a, rng)
+    fill_random(b, rng)
+    fill_random(c, rng)
+    api.contract(alpha, a, b, beta, c, ia, ib, ic)
+    out = canon(c)
+    for t in (a, b, c):
+        t.free()
+    return out
+
+
+PAIR_CB = C.CFUNCTYPE(None, C.c_size_t, C.c_double, C.c_double, C.c_long, C.c_long, C.c_long)
+
+
+def pair_structure_oracle(lib, a, b, c, ia, ib, ic):
+    """Merged pair list of the oracle (pair callback during xm_contract)."""
+    out = []
+
+    def cb(l, re, im, m, n, k):
+        out.append((int(l), complex(re, im), int(m), int(n), int(k)))
+    f = PAIR_CB(cb)
+    lib.dll.xmo_set_pair_callback.argtypes = [PAIR_CB]
+    lib.dll.xmo_set_pair_callback(f)
+    api.contract(1.0, a, b, 0.0, c, ia, ib, ic)
+    lib.dll.xmo_set_pair_callback(PAIR_CB())
+    return sorted(out, key=lambda x: (x[0], x[4], x[2], x[3], x[1].real, x[1].imag))
+
+
+def pair_structure_engine(lib, a, b, c, ia, ib, ic):
+    out = []
+
+    def cb(l, re, im, m, n, k):
+        out.append((int(l), complex(re, im), int(m), int(n), int(k)))
+    f = PAIR_CB(cb)
+    lib.dll.xmg_contract_pairs.argtypes = [C.c_void_p] * 3 + [C.c_char_p] * 3 + [PAIR_CB]
+    lib.check(lib.dll.xmg_contract_pairs(a.h, b.h, c.h, ia.encode(), ib.encode(), ic.encode(), f))
+    return sorted(out, key=lambda x: (x[0], x[4], x[2], x[3], x[1].real, x[1].imag))

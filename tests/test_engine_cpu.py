@@ -1,0 +1,169 @@
+"""Engine checks that need no GPU: the C-ABI library loads and exports every
+declared symbol, and its host planner reproduces the reference's block
+structure bit for bit (merged pair lists, factors, GEMM shapes, flops),
+driven through a pagefile allocator so that no device memory is touched."""
+import os
+import re
+import tempfile
+
+import numpy as np
+import pytest
+
+import cases
+import helpers as H
+from libxm_gb300 import api, workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        txt = open(os.path.join(ROOT, "include", h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"\b(xmg?_[a-z0-9_]+)\s*\(", txt):
+            names.add(m.group(1))
+    names -= {"xmg_pair_cb"}
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(engine):
+    names = declared_functions()
+    assert len(names) > 100
+    missing = [n for n in names if not hasattr(engine.dll, n)]
+    assert missing == []
+
+
+def test_exports_reference_test_driver_privates(engine):
+    # test.c calls xm_fatal and xm_make_masks (util.h:34-35)
+    assert hasattr(engine.dll, "xm_fatal") and hasattr(engine.dll, "xm_make_masks")
+    assert api.make_masks(engine, "ijcd", "cdab") == ([2, 3], [0, 1])
+
+
+def test_engine_blockspace_kat(engine):
+    bs = api.BlockSpace(engine, [10, 20, 30, 40, 50, 60, 70, 80]).autosplit()
+    assert bs.nblocks() == [1, 1, 1, 2, 2, 2, 3, 3]
+    bs.free()
+    bs = api.BlockSpace(engine, [30, 31, 32, 33, 34]).autosplit()
+    assert bs.block_dims([0] * 5) == [30, 31, 32, 16, 18]
+    bs.free()
+    bs = api.BlockSpace(engine, [1000]).autosplit()
+    o = api.BlockSpace(engine, [1000])
+    lib_o = None
+    bs.free(); o.free()
+
+
+@pytest.fixture()
+def pagefile(engine):
+    d = tempfile.mkdtemp()
+    al = api.Allocator(engine, os.path.join(d, "xmpagefile"))
+    yield al
+    al.destroy()
+    os.rmdir(d)
+
+
+def test_autosplit_matches_oracle(engine, oracle):
+    for n in [1, 7, 31, 32, 33, 63, 64, 65, 100, 127, 129, 384, 1000, 1934, 4097]:
+        x = api.BlockSpace(engine, [n]).autosplit()
+        y = api.BlockSpace(oracle, [n]).autosplit()
+        assert x.nblocks() == y.nblocks()
+        nb = x.nblocks()[0]
+        assert [engine.xm_block_space_get_split(x.h, 0, i) for i in range(nb + 1)] == \
+               [oracle.xm_block_space_get_split(y.h, 0, i) for i in range(nb + 1)]
+        x.free(); y.free()
+
+
+def test_tensor_structure_on_pagefile(engine, pagefile):
+    a, b, c = cases.make_abc_9(engine, pagefile, api.DOUBLE)
+    blocks = c.canonical_blocks()
+    assert blocks == sorted(blocks, key=lambda x: x[::-1])  # index 0 fastest
+    assert a.block_type((1, 0, 0, 0)) == api.DERIVATIVE
+    assert a.block_perm((1, 0, 0, 0)) == [1, 0, 2, 3]
+    assert a.block_scalar((1, 0, 0, 0)) == -1
+    assert a.data_ptr((1, 0, 0, 0)) == a.data_ptr((0, 1, 0, 0))
+    # pagefile round trip (no device involved)
+    blk = blocks[3]
+    v = np.arange(c.block_size(blk), dtype=np.float64)
+    c.write_block(blk, v)
+    assert np.array_equal(c.read_block(blk), v)
+    for t in (a, b, c):
+        t.free()
+
+
+@pytest.mark.parametrize("ci", range(len(cases.CONTRACT_TESTS)))
+def test_pair_structure_matches_oracle(engine, oracle, pagefile, ci):
+    make, ia, ib, ic = cases.CONTRACT_TESTS[ci]
+    ao = api.Allocator(oracle)
+    for dt in H.TYPES:
+        a, b, c = make(engine, pagefile, dt)
+        mine = H.pair_structure_engine(engine, a, b, c, ia, ib, ic)
+        flops = engine.xmg_contract_flops(a.h, b.h, c.h, ia.encode(), ib.encode(), ic.encode())
+        for t in (a, b, c):
+            t.free()
+        x, y, z = make(oracle, ao, dt)
+        for t in (x, y, z):
+            H.fill_random(t, np.random.default_rng(1))
+        ref = H.pair_structure_oracle(oracle, x, y, z, ia, ib, ic)
+        for t in (x, y, z):
+            t.free()
+        assert mine == ref
+        mult = 8 if dt in (1, 3) else 2
+        assert flops == sum(mult * m * n * k for _, _, m, n, k in ref)
+
+
+@pytest.mark.parametrize("name", ["cfg1", "cfg2"])
+def test_workload_structure_matches_oracle(engine, oracle, pagefile, name):
+    """Full-size block structure of the measured ladders, bit-exact."""
+    gen = {"cfg1": W.cfg1, "cfg2": W.cfg2}[name]
+    oracle.dll.xmo_set_plan_only(1)
+    try:
+        ws = []
+        for lib, al in ((engine, pagefile), (oracle, api.Allocator(oracle))):
+            orig_fill = W.fill
+            W.fill = lambda *a, **k: None      # structure only: no data
+            try:
+                ws.append(gen(lib, al))
+            finally:
+                W.fill = orig_fill
+        e, o = ws
+        mine = H.pair_structure_engine(engine, e.a, e.b, e.c, e.idxa, e.idxb, e.idxc)
+        ref = H.pair_structure_oracle(oracle, o.a, o.b, o.c, o.idxa, o.idxb, o.idxc)
+        assert len(mine) > 0 and mine == ref
+        flops = engine.xmg_contract_flops(e.a.h, e.b.h, e.c.h, b"ijcd", b"cdab", b"ijab")
+        assert flops == sum(2 * m * n * k for _, _, m, n, k in ref)
+        if name == "cfg1":
+            assert len(e.c.canonical_blocks()) == 60 and len(ref) == 600
+            assert flops == 5033164800.0
+        for w in ws:
+            for t in w.tensors():
+                t.free(data=True)
+    finally:
+        oracle.dll.xmo_set_plan_only(0)
+
+
+def test_golden_gemm_log_cfg1(engine, pagefile):
+    """The engine's cfg1 plan against the reference's recorded GEMM calls."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+    orig = W.fill
+    W.fill = lambda *a, **k: None
+    try:
+        w = W.cfg1(engine, pagefile)
+    finally:
+        W.fill = orig
+    mine = H.pair_structure_engine(engine, w.a, w.b, w.c, w.idxa, w.idxb, w.idxc)
+    log = g["cfg1_log"]
+    assert sorted((min(m, n), max(m, n), k, z.real) for _, z, m, n, k in mine) == \
+        sorted((int(min(r[1], r[2])), int(max(r[1], r[2])), int(r[3]), r[4]) for r in log)
+    w.free()
+
+
+def test_invalid_indices_return_status(engine, pagefile):
+    a, b, c = cases.make_abc_1(engine, pagefile, api.DOUBLE)
+    st = engine.xmg_contract(api.Scalar.of(1), a.h, b.h, api.Scalar.of(0), c.h, b"ik", b"kj", b"ijx")
+    assert st == 1 and b"bad contraction indices" in engine.xmg_last_error()
+    st = engine.xmg_contract(api.Scalar.of(1), a.h, b.h, api.Scalar.of(0), c.h, b"ik", b"kj", b"jk")
+    assert st == 1
+    for t in (a, b, c):
+        t.free()
