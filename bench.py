@@ -1,0 +1,430 @@
+#!/usr/bin/env python3
+"""Benchmark: xm_contract TFLOP/s on one GB300, split-precision (emulated
+FP64 on tcgen05 tensor cores) against the plain FP64 GPU form, with the
+relative Frobenius error of both against FP64 references.
+
+Workload: the uneven-block, Z2^3-sparse FP64 ladder
+    C(i,j,a,b) = sum_{c,d} A(i,j,c,d) B(c,d,a,b)
+o = 96 in 6 blocks of 8..24, v = 384 in 12 blocks of 16..48, i<->j, c<->d,
+a<->b antisymmetry, seeded uniform[-1,1] data (synthetic: splitmix64).
+Inputs (A ~0.3 GB, B ~5.4 GB) are larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+One step = one xm_contract call over the whole workload (plan + kernels +
+synchronisation) with block data resident in HBM.  e2e = the same step
+through the C API with host buffers: every canonical block of A and B
+written from page-locked host memory, the contraction, every canonical
+block of C read back.  For N > 1 (torchrun) every rank runs an independent
+replica on its own GPU (no collective on the data path; weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+import numpy as np  # noqa: E402
+
+METRIC = "xm_contract TFLOP/s on 1 GB300: split-precision vs plain FP64 at rel err ≤1e-12"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- ranks --
+class Ranks:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            import torch.distributed as dist
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)])
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+# --------------------------------------------------------------- clocks --
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev, self.rows, self.proc = dev, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 7
+                          for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm),
+                "power_w_max": max((float(r[2]) for r in self.rows if len(r) >= 7
+                                    and r[2].replace(".", "").isdigit()), default=None)}
+
+
+# ------------------------------------------------------------- CPU side --
+def cpu_lib():
+    """The reference built from source when it loads on this machine, else
+    the oracle port.  Returns (lib, kind)."""
+    import oracle.build as ob
+    from libxm_gb300 import api
+    blas = ob.find_blas()
+    ref = ob.build_reference()
+    if ref is not None:
+        try:
+            lib = api.Lib(ref)
+            lib.dll.xmref_set_blas.argtypes = [api.C.c_char_p]
+            lib.dll.xmref_set_blas(blas.encode() if blas else None)
+            return lib, "reference"
+        except OSError:
+            pass
+    lib = api.Lib(ob.build_oracle())
+    lib.dll.xmo_set_blas.argtypes = [api.C.c_char_p]
+    lib.dll.xmo_set_blas(blas.encode() if blas else None)
+    return lib, "port"
+
+
+def cpu_baseline(w, ranks, target_s, engine_out=None):
+    """Time the CPU reference on a bounded sample of the workload's output
+    blocks: all host threads, OPENBLAS_NUM_THREADS=1 (it parallelises over
+    blocks itself)."""
+    from libxm_gb300 import api, workloads as W
+    lib, kind = cpu_lib()
+    al = api.Allocator(lib)
+    wc = make_workload(lib, al, w.scale)
+    blocks = wc.c.canonical_blocks()
+    cost = block_costs(wc)
+
+    def run_sample(nblk):
+        chosen = set(blocks[:nblk])
+        c = wc.c.structure()
+        for blk in blocks:
+            if blk not in chosen:
+                lib.xm_tensor_set_zero_block(c.h, api.Dim.of(blk))
+        fl = sum(cost[i] for i in range(nblk))
+        t0 = time.perf_counter()
+        api.contract(wc.alpha, wc.a, wc.b, wc.beta, c, wc.idxa, wc.idxb, wc.idxc)
+        dt = time.perf_counter() - t0
+        out = {blk: c.read_block(blk) for blk in c.canonical_blocks()}
+        c.free()
+        return fl, dt, out
+
+    n = max(1, len(blocks) // 50)
+    fl, dt, _ = run_sample(n)
+    rate = fl / max(dt, 1e-6)
+    total = sum(cost)
+    want = min(total, rate * target_s)
+    acc, nblk = 0.0, 0
+    while nblk < len(blocks) and acc < want:
+        acc += cost[nblk]
+        nblk += 1
+    fl, dt, out = run_sample(nblk)
+    threads = lib.dll.xmo_num_threads() if hasattr(lib.dll, "xmo_num_threads") else os.cpu_count()
+    res = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": int(os.environ.get("OMP_NUM_THREADS", threads or os.cpu_count())),
+           "kind": kind,
+           "sample": "%d of %d canonical output blocks (%.3e of %.3e useful flops), %.1f s"
+                     % (nblk, len(blocks), fl, total, dt)}
+    wc.free()
+    return res, out
+
+
+def block_costs(w):
+    """Useful flops per canonical output block (the reference's GEMM work)."""
+    import oracle.build as ob
+    from libxm_gb300 import api
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    lib = w.c.lib
+    blocks = w.c.canonical_blocks()
+    cost = [0.0] * len(blocks)
+    if lib.gb:
+        import helpers as H
+        for l, _, m, n, k in H.pair_structure_engine(lib, w.a, w.b, w.c, w.idxa, w.idxb, w.idxc):
+            cost[l] += 2.0 * m * n * k
+        return cost
+    # plan-only pass of the oracle on the same structure
+    orc = api.Lib(ob.build_oracle())
+    oal = api.Allocator(orc)
+    from libxm_gb300 import workloads as W
+    orig = W.fill
+    W.fill = lambda *x, **y: None
+    try:
+        wo = make_workload(orc, oal, w.scale)
+    finally:
+        W.fill = orig
+    import helpers as H
+    orc.dll.xmo_set_plan_only(1)
+    for l, _, m, n, k in H.pair_structure_oracle(orc, wo.a, wo.b, wo.c, wo.idxa, wo.idxb, wo.idxc):
+        cost[l] += 2.0 * m * n * k
+    orc.dll.xmo_set_plan_only(0)
+    wo.free()
+    return cost
+
+
+def make_workload(lib, al, scale=1):
+    from libxm_gb300 import workloads as W
+    w = W.cfg2(lib, al, scale=scale)
+    w.scale = scale
+    return w
+
+
+# --------------------------------------------------------------- engine --
+def engine_arm(args, ranks):
+    os.environ.setdefault("XMG_DEVICE", str(ranks.local))
+    import libxm_gb300
+    from libxm_gb300 import api, workloads as W
+    libxm_gb300.build()
+    eng = libxm_gb300.load()
+    al = api.Allocator(eng)
+    t0 = time.perf_counter()
+    w = make_workload(eng, al, args.scale)
+    setup_s = time.perf_counter() - t0
+    flops = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+
+    def timed(prec, steps, warmup):
+        eng.check(eng.xmg_set_precision(prec))
+        for _ in range(warmup):
+            w.run()
+        ranks.barrier()
+        eng.check(eng.xmg_synchronize())
+        clk = Clocks(int(os.environ["XMG_DEVICE"]))
+        clk.start()
+        n0 = eng.xmg_kernel_launches()
+        gemm_ms, split_ms = [], []
+        eng.check(eng.xmg_timer_start())
+        for _ in range(steps):
+            w.run()
+            st = api.last_stats(eng)
+            gemm_ms.append(st.ms_gemm)
+            split_ms.append(st.ms_split)
+        ms = eng.xmg_timer_stop()
+        eng.check(eng.xmg_synchronize())
+        launches = eng.xmg_kernel_launches() - n0
+        ranks.barrier()
+        clocks = clk.stop()
+        ms = ranks.max(ms)
+        return {"ms_per_step": ms / steps, "gemm_ms": float(np.mean(gemm_ms)),
+                "split_ms": float(np.mean(split_ms)), "launches": launches // steps,
+                "clocks": clocks, "precision_used": api.last_stats(eng).precision_used,
+                "out": W.read_canonical(w.c)}
+
+    emu = timed(api.PREC_AUTO, args.steps, args.warmup)
+    fp64 = timed(api.PREC_FP64, args.fp64_steps, 1)
+    rel_emu_vs_fp64 = W.rel_frobenius(emu["out"], fp64["out"])
+
+    # e2e through the C API with page-locked host buffers
+    e2e = None
+    if True:
+        eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+        host = {}
+        nbytes_in = nbytes_out = 0
+        for t in (w.a, w.b):
+            for blk in t.canonical_blocks():
+                n = t.block_size(blk) * 8
+                p = eng.xmg_host_alloc(n)
+                buf = np.frombuffer((api.C.c_char * n).from_address(p), dtype=np.float64)
+                buf[:] = t.read_block(blk)
+                host[(id(t), blk)] = (p, buf)
+                nbytes_in += n
+        outs = {}
+        for blk in w.c.canonical_blocks():
+            n = w.c.block_size(blk) * 8
+            p = eng.xmg_host_alloc(n)
+            outs[blk] = (p, n)
+            nbytes_out += n
+        steps = max(1, min(args.steps, 3))
+
+        def e2e_step():
+            for t in (w.a, w.b):
+                for blk in t.canonical_blocks():
+                    eng.xm_tensor_write_block(t.h, api.Dim.of(blk), host[(id(t), blk)][0])
+            w.run()
+            for blk, (p, n) in outs.items():
+                eng.xm_tensor_read_block(w.c.h, api.Dim.of(blk), p)
+        e2e_step()
+        ranks.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            e2e_step()
+        dt = ranks.max((time.perf_counter() - t0) / steps)
+        e2e = {"value": ranks.world * flops / dt / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": nbytes_out,
+               "ms_per_step": dt * 1e3}
+        for p, _ in host.values():
+            eng.xmg_host_free(p)
+        for p, _ in outs.values():
+            eng.xmg_host_free(p)
+
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    tc_peak = peaks.get("bf16_tflops", 1900.0)
+    slices = 6
+    products = slices * (slices + 1) // 2
+    if emu["precision_used"] == api.PREC_EMU64 and emu["gemm_ms"] > 0:
+        achieved = flops * products / (emu["gemm_ms"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                "frac": achieved / tc_peak, "traffic": None,
+                "kernel": "emu_gemm (bf16 slices, tcgen05)",
+                "note": "achieved = useful FP64 flops x %d slice products / mean GEMM-kernel time; peak = measured cuBLAS bf16 burst" % products}
+    else:
+        achieved = flops / (emu["gemm_ms"] * 1e-3) / 1e12 if emu["gemm_ms"] > 0 else None
+        roof = {"bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "kernel": "plain_gemm_kernel<double>"}
+
+    cpu = None
+    rel_emu_vs_cpu = None
+    if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
+        cpu, cpu_out = cpu_baseline(w, ranks, args.cpu_seconds)
+        sub = {k: emu["out"][k] for k in cpu_out}
+        rel_emu_vs_cpu = W.rel_frobenius(sub, cpu_out)
+        rel_fp64_vs_cpu = W.rel_frobenius({k: fp64["out"][k] for k in cpu_out}, cpu_out)
+    value = ranks.world * flops / (emu["ms_per_step"] * 1e-3) / 1e12
+    fp64_value = ranks.world * flops / (fp64["ms_per_step"] * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": emu["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (emulated: bf16 slices, fp32 exact partials, int64 accumulation)",
+        "data": "synthetic (seeded splitmix64 uniform[-1,1]; inputs larger than L2)",
+        "config": {"workload": w.name, "o": w.extra["o_sizes"], "v": w.extra["v_sizes"],
+                   "z2_labels": {"o": w.extra["o_labels"], "v": w.extra["v_labels"]},
+                   "contraction": "C(ijab)=A(ijcd)B(cdab)", "useful_flops": flops,
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
+        "fp64_plain": {"value": fp64_value, "ms_per_step": fp64["ms_per_step"],
+                       "gemm_ms": fp64["gemm_ms"]},
+        "speedup_vs_fp64_plain": value / fp64_value,
+        "rel_err": {"emu_vs_gpu_fp64": rel_emu_vs_fp64, "emu_vs_cpu_fp64_sample": rel_emu_vs_cpu,
+                    "gpu_fp64_vs_cpu_fp64_sample": rel_fp64_vs_cpu if cpu else None},
+        "precision_used": "emu64" if emu["precision_used"] == api.PREC_EMU64 else "fp64",
+        "phases_ms": {"gemm": emu["gemm_ms"], "split": emu["split_ms"]},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": emu["launches"], "clocks": emu["clocks"],
+        "setup_s": setup_s,
+    }
+    if ranks.rank == 0:
+        print(json.dumps(line))
+
+
+def reference_arm(args, ranks):
+    if ranks.rank != 0:
+        return
+    from libxm_gb300 import api, workloads as W
+    lib, kind = cpu_lib()
+    al = api.Allocator(lib)
+    w = make_workload(lib, al, args.scale)
+    cost = block_costs(w)
+    blocks = w.c.canonical_blocks()
+    total = sum(cost)
+    # calibrate a per-step sample of roughly cpu-seconds / steps
+    per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
+
+    def make_c(nblk):
+        c = w.c.structure()
+        for blk in blocks[nblk:]:
+            lib.xm_tensor_set_zero_block(c.h, api.Dim.of(blk))
+        return c, sum(cost[:nblk])
+    c, fl = make_c(max(1, len(blocks) // 50))
+    t0 = time.perf_counter()
+    api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
+    rate = fl / max(time.perf_counter() - t0, 1e-6)
+    c.free()
+    acc, nblk = 0.0, 0
+    while nblk < len(blocks) and acc < rate * per_step:
+        acc += cost[nblk]
+        nblk += 1
+    c, fl = make_c(nblk)
+    for _ in range(args.warmup):
+        api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = fl / dt / 1e12
+    threads = os.environ.get("OMP_NUM_THREADS") or os.cpu_count()
+    sample = "%d of %d canonical output blocks (%.3e of %.3e useful flops) per step" % (
+        nblk, len(blocks), fl, total)
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64 uniform[-1,1])",
+        "config": {"workload": w.name, "contraction": "C(ijab)=A(ijcd)B(cdab)",
+                   "useful_flops_total": total, "parallelism": "host threads"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": int(threads), "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }))
+    c.free()
+    w.free()
+
+
+def main():
+    args = parse()
+    ranks = Ranks()
+    if args.impl == "reference":
+        reference_arm(args, ranks)
+    else:
+        engine_arm(args, ranks)
+
+
+if __name__ == "__main__":
+    main()

@@ -101,6 +101,22 @@ int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
 
+/* Device-time measurement on the engine's stream: start records an event,
+ * stop records another, waits for it and returns the elapsed milliseconds
+ * (negative on error). */
+int xmg_timer_start(void);
+double xmg_timer_stop(void);
+
+/* Number of engine kernels launched since the library was loaded. */
+long long xmg_kernel_launches(void);
+
+/* Page-locked host buffers for fast block transfers (NULL on failure). */
+void *xmg_host_alloc(size_t bytes);
+void xmg_host_free(void *p);
+
+/* The engine runs on device ordinal $XMG_DEVICE (default 0), chosen at
+ * the first call that needs the GPU. */
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

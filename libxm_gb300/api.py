@@ -124,6 +124,11 @@ _GB_SIGS = {
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
     "xm_contract_adjoint": (C.c_int, [Scalar, _P, _P, _P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p]),
+    "xmg_timer_start": (C.c_int, []),
+    "xmg_timer_stop": (C.c_double, []),
+    "xmg_kernel_launches": (C.c_longlong, []),
+    "xmg_host_alloc": (_P, [C.c_size_t]),
+    "xmg_host_free": (None, [_P]),
 }
 
 

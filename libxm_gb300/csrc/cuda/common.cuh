@@ -16,6 +16,7 @@ namespace xmg {
 cudaStream_t stream();          /* engine compute stream */
 int num_sms();
 int check(cudaError_t e, const char *what);
+extern long long g_launches;     /* kernels launched by the engine */
 #define XMG_CK(call) do { int _s = xmg::check((call), #call); if (_s) return _s; } while (0)
 
 /* element types: xm_scalar_type_t order */

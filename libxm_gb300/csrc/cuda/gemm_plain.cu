@@ -143,6 +143,7 @@ plain_gemm_launch(const void *items, int nitems, const xmgd_cblock_t *cbs,
 		return XMG_OK;
 	plain_gemm_kernel<T><<<nitems, PG_THREADS, 0, stream()>>>(
 	    (const pg_item *)items, cbs, prs, tabs, make_double2(beta[0], beta[1]));
+	g_launches++;
 	return check(cudaGetLastError(), "plain_gemm_kernel launch");
 }
 

@@ -162,7 +162,8 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		for (int e = threadIdx.x; e < TILE * TILE; e += PT_THREADS) {
 			int i0 = e % TILE, i1 = e / TILE;
 			if (i0 < w0 && i1 < w1) {
-				D *dp = dst + od + (b0 + i0) + (b1 + i1) * t.dst_stride[1];
+				D *dp = dst + od + (b0 + i0) * t.dst_stride[0] +
+				    (b1 + i1) * t.dst_stride[1];
 				elem_op<D, S>::apply(op, dp, &tile[i1][i0], al, als, be,
 				    dre, dim_);
 			}
@@ -198,6 +199,7 @@ launch(const xmgd_ptask_t *dtasks, const task_meta *dmeta, int ntasks,
 	/* grid.x limit is 2^31-1; batches are far smaller */
 	ptask_kernel<D, S><<<(unsigned)nctas, PT_THREADS, 0, stream()>>>(
 	    dtasks, dmeta, ntasks, dpartial);
+	g_launches++;
 	return check(cudaGetLastError(), "ptask_kernel launch");
 }
 

@@ -17,6 +17,8 @@ static int g_dev = 0;
 static int g_sms = 0;
 static cudaStream_t g_stream = nullptr;
 static size_t g_in_use = 0;
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+long long g_launches = 0;
 
 struct buf { void *p; size_t n; };
 static buf g_scratch[XMGD_SCRATCH_SLOTS];
@@ -48,13 +50,19 @@ xmgd_init(void)
 	cudaMemPool_t pool;
 	uint64_t thr = UINT64_MAX;
 
+	const char *dev;
+
 	if (g_ready)
 		return XMG_OK;
+	if ((dev = getenv("XMG_DEVICE")) != NULL)
+		g_dev = atoi(dev);
 	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
 		cudaGetLastError();
 		return xmg_seterr(XMG_ECUDA, "no CUDA device available: the "
 		    "libxm-gb300 engine runs its kernels on the GPU only");
 	}
+	if (g_dev < 0 || g_dev >= n)
+		return xmg_seterr(XMG_EINVAL, "XMG_DEVICE=%d out of range", g_dev);
 	XMG_CK(cudaSetDevice(g_dev));
 	XMG_CK(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount,
 	    g_dev));
@@ -176,4 +184,50 @@ xmgd_pinned(size_t bytes, void **hptr)
 	}
 	*hptr = g_pinned.p;
 	return XMG_OK;
+}
+
+extern "C" int
+xmg_timer_start(void)
+{
+	int st;
+
+	if ((st = xmgd_init()) != XMG_OK)
+		return st;
+	if (!g_t0) {
+		XMG_CK(cudaEventCreate(&g_t0));
+		XMG_CK(cudaEventCreate(&g_t1));
+	}
+	XMG_CK(cudaEventRecord(g_t0, g_stream));
+	return XMG_OK;
+}
+
+extern "C" double
+xmg_timer_stop(void)
+{
+	float ms = -1;
+
+	if (!g_t0 || cudaEventRecord(g_t1, g_stream) != cudaSuccess ||
+	    cudaEventSynchronize(g_t1) != cudaSuccess ||
+	    cudaEventElapsedTime(&ms, g_t0, g_t1) != cudaSuccess)
+		return -1.0;
+	return ms;
+}
+
+extern "C" long long xmg_kernel_launches(void) { return g_launches; }
+
+extern "C" void *
+xmg_host_alloc(size_t bytes)
+{
+	void *p = nullptr;
+
+	if (xmgd_init() != XMG_OK || cudaMallocHost(&p, bytes) != cudaSuccess)
+		return nullptr;
+	return p;
+}
+
+extern "C" void
+xmg_host_free(void *p)
+{
+	if (p)
+		cudaFreeHost(p);
 }

@@ -443,6 +443,10 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			p->flops += mult * cb->m * (double)cb->n * pr->k;
 			if (!pow2_factor(cand[i].al, &sign, &shift))
 				emu = 0;
+			else {
+				pr->esign = sign;
+				pr->eshift = shift;
+			}
 			if (!device)
 				continue;
 			xmg_tensor_block_strides(a, cand[i].ia, sa);

@@ -76,6 +76,8 @@ typedef struct {
 	int32_t k;
 	int32_t arow, acol, brow, bcol;
 	int32_t aview, bview;        /* operand-view ids (emulation) */
+	int32_t esign, eshift;       /* pair factor = esign * 2^eshift when
+	                                it is a signed power of two */
 	double al[2];
 } xmgd_pair_t;
 
@@ -85,7 +87,8 @@ typedef struct {
 	int32_t k, mn;               /* rows (contracted), cols (free) */
 	int32_t rowtab, coltab;      /* table-pool offsets */
 	int32_t exptab;              /* exponent-table offset (per column) */
-	int32_t pad;
+	int32_t n_rt, n_ks;          /* 128-row tiles, 16-wide K steps */
+	int32_t kfast;               /* rows (K) unit-stride in memory */
 	uint64_t slices;             /* device address of the tiled slices */
 } xmgd_view_t;
 
