@@ -64,14 +64,24 @@ xmg_get_last_stats(xmg_stats_t *out)
 typedef struct {
 	int32_t *v;
 	int64_t n, cap;
-	xmg_hmap_t index;        /* descriptor hash -> offset */
+	xmg_hmap_t index;        /* descriptor hash -> descriptor slot */
+	struct tabdesc {
+		int nd;
+		int64_t size[XM_MAX_DIM], stride[XM_MAX_DIM];
+		int32_t off;
+	} *desc;
+	int ndesc, capdesc;
 } tabpool_t;
 
+/* Offset table sum_d digit_d(e) * stride[d] (first dimension fastest),
+ * interned by its (sizes, strides) descriptor: blocks of equal shape and
+ * permutation share one table. */
 static int32_t
 tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 {
-	uint64_t h = 0x9e3779b97f4a7c15ULL, off;
+	uint64_t h = 0x9e3779b97f4a7c15ULL, slot;
 	int64_t total = 1, e, r, o;
+	struct tabdesc *t;
 	int d;
 
 	for (d = 0; d < nd; d++) {
@@ -80,30 +90,35 @@ tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 		total *= size[d];
 	}
 	h = xmg_hash64(h ^ (uint64_t)nd);
-	if (h == XMG_HMAP_EMPTY)
-		h--;
-	if (xmg_hmap_get(&p->index, h, &off)) {
-		/* verify: recompute and compare (hash collisions are
-		 * astronomically rare, but never silently wrong) */
-		int same = 1;
-		for (e = 0; e < total && same; e++) {
-			r = e; o = 0;
-			for (d = 0; d < nd; d++) {
-				o += (r % size[d]) * stride[d];
-				r /= size[d];
-			}
-			same = off + (uint64_t)e < (uint64_t)p->n &&
-			    p->v[off + e] == (int32_t)o;
-		}
-		if (same)
-			return (int32_t)off;
+	for (;;) {
+		if (h == XMG_HMAP_EMPTY)
+			h--;
+		if (!xmg_hmap_get(&p->index, h, &slot))
+			break;
+		t = &p->desc[slot];
+		if (t->nd == nd &&
+		    memcmp(t->size, size, (size_t)nd * sizeof *size) == 0 &&
+		    memcmp(t->stride, stride, (size_t)nd * sizeof *stride) == 0)
+			return t->off;
+		h = xmg_hash64(h + 1);	/* collision: probe another key */
 	}
 	while (p->n + total > p->cap) {
 		p->cap = p->cap ? 2 * p->cap : 4096;
 		if ((p->v = realloc(p->v, (size_t)p->cap * sizeof *p->v)) == NULL)
 			xm_fatal("%s: out of memory", __func__);
 	}
-	off = (uint64_t)p->n;
+	if (p->ndesc == p->capdesc) {
+		p->capdesc = p->capdesc ? 2 * p->capdesc : 256;
+		if ((p->desc = realloc(p->desc, (size_t)p->capdesc *
+		    sizeof *p->desc)) == NULL)
+			xm_fatal("%s: out of memory", __func__);
+	}
+	t = &p->desc[p->ndesc];
+	memset(t, 0, sizeof *t);
+	t->nd = nd;
+	memcpy(t->size, size, (size_t)nd * sizeof *size);
+	memcpy(t->stride, stride, (size_t)nd * sizeof *stride);
+	t->off = (int32_t)p->n;
 	for (e = 0; e < total; e++) {
 		r = e; o = 0;
 		for (d = 0; d < nd; d++) {
@@ -112,8 +127,8 @@ tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 		}
 		p->v[p->n++] = (int32_t)o;
 	}
-	xmg_hmap_put(&p->index, h, off);
-	return (int32_t)off;
+	xmg_hmap_put(&p->index, h, (uint64_t)p->ndesc);
+	return p->desc[p->ndesc++].off;
 }
 
 /* Table over the masked dimensions of a block with the given strides. */
@@ -162,6 +177,7 @@ static void
 plan_free(plan_t *p)
 {
 	free(p->cb); free(p->pr); free(p->va); free(p->vb); free(p->tabs.v);
+	free(p->tabs.desc);
 	free(p->emulatable);
 	xmg_hmap_free(&p->tabs.index);
 	xmg_hmap_free(&p->va_index); xmg_hmap_free(&p->vb_index);
