@@ -98,6 +98,28 @@ int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
     const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,
     xm_tensor_t *db, const char *idxa, const char *idxb, const char *idxc);
 
+/* Allocation-free dot product.  No counterpart in the reference: it is an
+ * addition for callers that cannot allocate memory at the point where they
+ * need the value -- typically a host program whose own pool already holds
+ * the GPU memory it may use (so any cudaMalloc would fail), or a solver
+ * evaluating a norm every iteration of a tight loop, where the regular
+ * xm_dot's first-use device allocations would stall it.  Same result as
+ * xm_dot(a, b, idxa, idxb), written to *result; the tensors must live in
+ * GPU memory (allocator created with path NULL).  It calls no cudaMalloc,
+ * cudaFree or host allocator: its task table, per-CTA partial sums and
+ * running result live in one static device array of about 270 KiB that
+ * every GPU loading the library keeps until exit.  Limits: blocks of at
+ * most XMG_NOALLOC_MAX_CTAS * XMG_NOALLOC_ELEMS_PER_CTA elements (larger
+ * ones are rejected with XMG_EINVAL), tasks run in batches of
+ * XMG_NOALLOC_MAX_TASKS.  The first call on a device looks up the array's
+ * device address and should come before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  Returns XMG_* status. */
+#define XMG_NOALLOC_MAX_TASKS      64
+#define XMG_NOALLOC_MAX_CTAS       16384
+#define XMG_NOALLOC_ELEMS_PER_CTA  2048
+int xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b,
+    const char *idxa, const char *idxb, xm_scalar_t *result);
+
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
 
