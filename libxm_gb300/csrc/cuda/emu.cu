@@ -181,6 +181,21 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
 		v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+	uint32_t r[16];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+	    "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]),
+	      "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+	      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+	      "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+	    : "r"(taddr));
+#pragma unroll
+	for (int i = 0; i < 16; i++)
+		v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_wait_ld()
 {
 	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -393,6 +408,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 			int s = 0;
 			uint32_t ph = 0;
 			int lastp[EMU_NST];
+#pragma unroll
 			for (int q = 0; q < EMU_NST; q++)
 				lastp[q] = -1;
 			for (int p = 0; p < cb.npairs && !s_err; p++) {
@@ -410,7 +426,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 					mbar_expect_tx(fb, STAGE_BYTES);
 					bulk_g2s(dst, gb + (size_t)ks * CHUNK_BYTES, CHUNK_BYTES, fb);
 					bulk_g2s(dst + CHUNK_BYTES, ga + (size_t)ks * CHUNK_BYTES, CHUNK_BYTES, fb);
-					lastp[s] = (int)ph;
+#pragma unroll
+					for (int q = 0; q < EMU_NST; q++)
+						if (q == s)
+							lastp[q] = (int)ph;
 					if (++s == EMU_NST) { s = 0; ph ^= 1; }
 				}
 			}
@@ -419,6 +438,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 			 * stage completes when its bytes have arrived */
 			if (s_err) {
 				uint64_t t0 = gtimer();
+#pragma unroll
 				for (int q = 0; q < EMU_NST; q++)
 					if (lastp[q] >= 0)
 						while (!mbar_try(smem_u32(&bar_full[q]), (uint32_t)lastp[q]) &&
@@ -441,6 +461,11 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 						eph ^= 1;
 					}
 					tc_fence_after();
+					/* every accumulator restarts each chunk: the exact
+					 * groups for their 2^23 bound, the low band because the
+					 * tensor core's fp32 accumulation error grows with the
+					 * accumulation length (per-pair accumulation measured
+					 * 10x larger error) */
 					uint32_t started = 0;
 					const int c1 = min(nks, c0 + EMU_CHUNK);
 					for (int ks = c0; ks < c1; ks++) {
@@ -476,7 +501,6 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 		/* ---------------- drain + epilogue (warps 2..9) ---------------- */
 		const int quad = warp & 3, half = (warp - 2) >> 2;
 		const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + half * 64;
-		const float sc3 = __int_as_float((127 + 16 + F) << 23);	/* 2^(16+F) */
 		long long V[64];
 #pragma unroll
 		for (int c = 0; c < 64; c++)
@@ -486,7 +510,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 		for (int p = 0; p < cb.npairs && ok; p++) {
 			const xmgd_pair_t pr = prs[cb.first_pair + p];
 			const int nks = vb[pr.bview].n_ks;
-			const int sign = pr.esign, shift = pr.eshift;
+			/* the pair factor sign * 2^shift (shift 0 or 1, checked by
+			 * the planner) rides on the exact fp32 -> int scales */
+			const float sg = pr.esign > 0 ? 1.0f : -1.0f;
+			const float s0 = sg * __int_as_float((127 + pr.eshift) << 23);
+			const float s1 = s0 * 256.0f, s2 = s0 * 65536.0f;
+			const float s3 = s0 * __int_as_float((127 + 16 + F) << 23);
 			for (int c0 = 0; c0 < nks; c0 += EMU_CHUNK) {
 				/* one lane waits, the warp follows its verdict, so the
 				 * .sync.aligned TMEM loads below stay convergent */
@@ -510,13 +539,13 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 					tmem_wait_ld();
 #pragma unroll
 					for (int c = 0; c < 8; c++) {
-						long long i0 = __float2int_rn(a0[c]);
-						long long i1 = __float2int_rn(a1[c] * 256.0f);
-						long long i2 = __float2int_rn(a2[c] * 65536.0f);
-						long long lo = __float2ll_rn(a3[c] * sc3);
-						long long d = (((i0 << 16) + (i1 << 8) + i2) << F) + lo;
-						d = shift >= 0 ? (d << shift) : (d >> -shift);
-						V[b8 * 8 + c] += sign > 0 ? d : -d;
+						/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
+						 * |i0 * 256 + i1| < 2^31 */
+						int i0 = __float2int_rn(a0[c] * s0);
+						int i1 = __float2int_rn(a1[c] * s1);
+						int i2 = __float2int_rn(a2[c] * s2);
+						long long d = ((long long)(i0 * 256 + i1) << 8) + i2;
+						V[b8 * 8 + c] += (d << F) + __float2ll_rn(a3[c] * s3);
 					}
 				}
 				tc_fence_before();

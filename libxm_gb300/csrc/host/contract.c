@@ -236,8 +236,8 @@ view_id(xmgd_view_t **arr, int *n, int *cap, xmg_hmap_t *index,
 	return (*n)++;
 }
 
-/* +-2^t with |t| <= 16, real: the emulated path folds such factors into
- * exact integer shifts. */
+/* +-1 or +-2, real: the emulated path folds such pair factors exactly into
+ * its integer drains (merged antisymmetric pairs give exactly these). */
 static int
 pow2_factor(xm_scalar_t s, int *sign, int *shift)
 {
@@ -247,7 +247,7 @@ pow2_factor(xm_scalar_t s, int *sign, int *shift)
 	if (cimag(s) != 0 || r == 0 || !isfinite(r))
 		return 0;
 	m = frexp(fabs(r), &e);
-	if (m != 0.5 || e - 1 < -16 || e - 1 > 16)
+	if (m != 0.5 || e - 1 < 0 || e - 1 > 1)
 		return 0;
 	*sign = r < 0 ? -1 : 1;
 	*shift = e - 1;
