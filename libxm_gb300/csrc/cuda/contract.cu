@@ -95,7 +95,7 @@ xmgd_contract(xmgd_contract_t *p)
 			continue;
 		}
 		bool want_emu = p->precision != XMG_PREC_FP64 &&
-		    p->emulatable[i] && p->dtype == 2 /* double */;
+		    p->emulatable[i];
 		(want_emu ? emu : plain).push_back(i);
 	}
 	if (!scale.empty() && (st = xmgd_ptasks(p->dtype, p->dtype,

@@ -1,0 +1,156 @@
+/*
+ * Inline-PTX helpers for Blackwell kernels: mbarriers with bounded waits,
+ * 1-D bulk copies, tcgen05 MMA / commit / TMEM loads, shared-memory
+ * matrix descriptors (no swizzle, K-major).
+ */
+#ifndef XMG_TC_CUH
+#define XMG_TC_CUH
+
+#include <stdint.h>
+
+namespace xmg {
+
+constexpr uint64_t WAIT_NS = 2000000000ull;	/* bounded waits: 2 s */
+
+/* tcgen05 instruction descriptor, kind::f16: D f32, A/B bf16, both
+ * K-major, N = 128 (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4) */
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+    ((uint32_t)(128 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+	return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t gtimer()
+{
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+	    :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+	    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+	return ok != 0;
+}
+
+/* Bounded wait; false on timeout or when another role already failed. */
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+    volatile int *s_err, int *g_err, int code)
+{
+	if (mbar_try(bar, parity))
+		return true;
+	uint64_t t0 = gtimer();
+	for (;;) {
+		if (mbar_try(bar, parity))
+			return true;
+		if (*s_err)
+			return false;
+		if (gtimer() - t0 > WAIT_NS) {
+			*s_err = code;
+			atomicMax(g_err, code);
+			return false;
+		}
+	}
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src,
+    uint32_t bytes, uint32_t bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes"
+	    " [%0], [%1], %2, [%3];" :: "r"(dst), "l"(src), "r"(bytes), "r"(bar)
+	    : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before()
+{
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after()
+{
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+/* shared-memory matrix descriptor: no swizzle, K-major core matrices of
+ * 8 rows x 16 bytes; LBO = 128 B between the two K-adjacent core matrices
+ * of a 16-wide K step, SBO = 256 B between 8-row groups; bits 46-48 = 1 */
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+	return (uint64_t)((saddr & 0x3FFFFu) >> 4) |
+	    ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+	    (1ull << 46);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b,
+    uint32_t acc)
+{
+	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+	    :: "r"(d), "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+	    :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+{
+	uint32_t r[8];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 "
+	    "{%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]),
+	      "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+	    : "r"(taddr));
+#pragma unroll
+	for (int i = 0; i < 8; i++)
+		v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+	uint32_t r[16];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+	    "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]),
+	      "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+	      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+	      "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+	    : "r"(taddr));
+#pragma unroll
+	for (int i = 0; i < 16; i++)
+		v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld()
+{
+	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+
+} /* namespace xmg */
+
+#endif

@@ -89,6 +89,9 @@ typedef struct {
 	int32_t exptab;              /* exponent-table offset (per column) */
 	int32_t n_rt, n_ks;          /* 128-row tiles, 16-wide K steps */
 	int32_t kfast;               /* rows (K) unit-stride in memory */
+	int32_t cplx;                /* complex elements: realified K */
+	int32_t khp;                 /* complex: K per half, padded to 16 */
+	int32_t pad2;
 	uint64_t slices;             /* device address of the tiled slices */
 } xmgd_view_t;
 

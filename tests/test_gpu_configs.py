@@ -1,0 +1,142 @@
+"""The remaining measured workloads as parity cases: the permuted ring term
+(float32 and complex128, beta = 1, pair-symmetric output) and the
+hand-written adjoint of the ladder (checked against the oracle's
+contractions and against finite differences of L = <dC, C>)."""
+import numpy as np
+import pytest
+
+import helpers as H
+from libxm_gb300 import api, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", [api.PREC_AUTO, api.PREC_FP64])
+@pytest.mark.parametrize("dtype,tol", [(api.FLOAT, 1e-6), (api.DOUBLE_COMPLEX, 1e-12),
+                                       (api.DOUBLE, 1e-12), (api.FLOAT_COMPLEX, 1e-6)])
+def test_ring_term(engine, oracle, dtype, tol, prec):
+    """C(i,a,j,b) += sum_{k,c} A(k,i,c,a) B(j,k,b,c) with 4 x 8 blocks of a
+    reduced size (same structure as the 64 / 256 configuration), against
+    an FP64 oracle on identical (for float types: float-rounded) inputs.
+    Plain FP32 accumulation is held to 1e-5; the split paths to 1e-6."""
+    engine.check(engine.xmg_set_precision(prec))
+    hi = {api.FLOAT: api.DOUBLE, api.FLOAT_COMPLEX: api.DOUBLE_COMPLEX}.get(dtype, dtype)
+    eal, oal = api.Allocator(engine), api.Allocator(oracle)
+    we = W.cfg3(engine, eal, dtype=dtype, o_blk=6, v_blk=10)
+    wo = W.cfg3(oracle, oal, dtype=hi, o_blk=6, v_blk=10)
+    for te, to in zip(we.tensors(), wo.tensors()):
+        for blk in te.canonical_blocks():
+            to.write_block(blk, te.read_block(blk).astype(api.NP_TYPES[hi]))
+    we.run()
+    wo.run()
+    rel = W.rel_frobenius(W.read_canonical(we.c), W.read_canonical(wo.c))
+    st = api.last_stats(engine)
+    we.free()
+    wo.free()
+    engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+    bound = tol if (prec == api.PREC_AUTO or dtype >= 2) else 1e-5
+    assert rel <= bound, (rel, st.precision_used)
+    if prec == api.PREC_AUTO:
+        assert st.precision_used == api.PREC_EMU64
+
+
+def _loss(lib, w, dc):
+    return api.dot(w.c, dc, w.idxc, w.idxc)
+
+
+def test_adjoint_ladder(engine, oracle):
+    """da, db from xm_contract_adjoint against (1) the oracle computing the
+    two gradient contractions and folding derivative blocks back in numpy,
+    (2) central differences of L = <dC, alpha * A * B>."""
+    alpha = 0.75
+    eal, oal = api.Allocator(engine), api.Allocator(oracle)
+    res = {}
+    for lib, al in ((engine, eal), (oracle, oal)):
+        w = W.cfg2(lib, al, scale=4)
+        w.alpha = alpha
+        dc = w.c.structure()
+        W.fill(dc, 77, W.LADDER_ANTISYM)
+        res[lib.path] = (w, dc)
+    (we, dce), (wo, dco) = res[engine.path], res[oracle.path]
+    da = we.a.structure()
+    db = we.b.structure()
+    api.set_all(da, 0)
+    api.set_all(db, 0)
+    engine.check(engine.xm_contract_adjoint(api.Scalar.of(alpha), we.a.h, we.b.h, dce.h,
+                                            da.h, db.h, b"ijcd", b"cdab", b"ijab"))
+    gda, gdb = W.read_canonical(da), W.read_canonical(db)
+
+    # (1) reference gradient with the oracle: W = mult * dc on canonical
+    # positions, G = alpha W B (resp. alpha A W) at every nonzero position,
+    # folded back through each block's permutation and scalar.
+    lib = oracle
+    nb = dco.nblocks()
+    wt = api.Tensor(lib, None, api.DOUBLE, oal,
+                    handle=lib.xm_tensor_create(lib.xm_tensor_get_block_space(dco.h), api.DOUBLE, oal.h))
+    mult = {}
+    for blk in np.ndindex(*nb):
+        if dco.block_type(blk) == api.ZERO:
+            continue
+        mult.setdefault(dco.data_ptr(blk), 0.0)
+        mult[dco.data_ptr(blk)] += dco.block_scalar(blk).real ** 2
+    for blk in dco.canonical_blocks():
+        wt.set_canonical(blk)
+        wt.write_block(blk, dco.read_block(blk) * mult[dco.data_ptr(blk)])
+
+    def full_grad_tensor(t):
+        g = api.Tensor(lib, None, api.DOUBLE, oal,
+                       handle=lib.xm_tensor_create(lib.xm_tensor_get_block_space(t.h), api.DOUBLE, oal.h))
+        for blk in np.ndindex(*t.nblocks()):
+            if t.block_type(blk) != api.ZERO:
+                g.set_canonical(blk)
+        return g
+
+    def fold(t, g):
+        out = {blk: np.zeros(t.block_size(blk)) for blk in t.canonical_blocks()}
+        ptr2canon = {t.data_ptr(blk): blk for blk in t.canonical_blocks()}
+        for blk in np.ndindex(*t.nblocks()):
+            if t.block_type(blk) == api.ZERO:
+                continue
+            q = ptr2canon[t.data_ptr(blk)]
+            dims = t.block_dims(blk)
+            perm = t.block_perm(blk)
+            x = g.read_block(blk).reshape(dims, order="F")
+            # element e of blk <-> element permute(e, perm) of q
+            y = np.transpose(x, np.argsort(perm))    # shape of q's block
+            out[q] += t.block_scalar(blk).real * y.ravel(order="F")
+        return out
+
+    ga = full_grad_tensor(wo.a)
+    api.contract(alpha, wt, wo.b, 0.0, ga, "ijab", "cdab", "ijcd")
+    ref_da = fold(wo.a, ga)
+    gb = full_grad_tensor(wo.b)
+    api.contract(alpha, wo.a, wt, 0.0, gb, "ijcd", "ijab", "cdab")
+    ref_db = fold(wo.b, gb)
+    assert W.rel_frobenius(gda, ref_da) <= 1e-11
+    assert W.rel_frobenius(gdb, ref_db) <= 1e-11
+
+    # (2) central differences on seeded canonical elements (L is linear in
+    # every element, so a unit step is exact up to rounding)
+    rng = np.random.default_rng(5)
+    wo.alpha = alpha
+    for t, grad in ((wo.a, ref_da), (wo.b, ref_db)):
+        blocks = t.canonical_blocks()
+        for _ in range(6):
+            blk = blocks[rng.integers(len(blocks))]
+            data = t.read_block(blk)
+            e = int(rng.integers(data.size))
+            vals = []
+            for h in (1.0, -1.0):
+                d2 = data.copy()
+                d2[e] += h
+                t.write_block(blk, d2)
+                wo.run()
+                vals.append(api.dot(wo.c, dco, "ijab", "ijab").real)
+            t.write_block(blk, data)
+            fd = (vals[0] - vals[1]) / 2.0
+            g_eng = (gda if t is wo.a else gdb)[blk][e]
+            assert abs(fd - g_eng) <= 1e-9 * max(1.0, abs(fd)), (fd, g_eng)
+    for x in (da, db, ga, gb, wt, dce, dco):
+        x.free()
+    we.free()
+    wo.free()
