@@ -34,7 +34,7 @@
  *  3. emu_gemm_kernel  - one CTA per (output block, 128 x 128 tile, pass);
  *     warp 0 streams stages with cp.async.bulk, warp 1 issues the slice
  *     products per 16-wide K step with tcgen05.mma.kind::f16 (bf16 x bf16 ->
- *     fp32) into TMEM accumulators, warps 2..9 drain them every 160 K
+ *     fp32) into TMEM accumulators, warps 2..17 drain them every 160 K
  *     elements (the exact groups stay below 3 * 160 * 2^14 < 2^23) into
  *     per-thread int64 fixed-point sums in units of 2^(-16-F), applying the
  *     pair factor exactly.  The epilogue is the only FP64 work:
@@ -60,7 +60,9 @@ constexpr int EMU_TM = 128;              /* rows per tile, both operands */
 constexpr int EMU_KS = 16;               /* K per stage = K per MMA */
 constexpr int EMU_CHUNK = 10;            /* K steps per exact chunk (160) */
 constexpr int SLICE_BYTES = EMU_TM * EMU_KS * 2;          /* 4096 */
-constexpr int GEMM_THREADS = 320;                         /* 10 warps */
+#ifndef EMU_DW
+#define EMU_DW 16                        /* drain warps: 8 or 16 */
+#endif
 constexpr int STAGE_BUDGET = 196608;                      /* 192 KiB */
 
 /* input element traits: slices, kept products, fixed-point bits */
@@ -94,8 +96,10 @@ template <> struct fin<float> {
 	{ return (int)((__float_as_uint(x) >> 23) & 0xff); }
 };
 
+/* one output tile: block, M-side (B view) row offset, N-side (A view) row
+ * offset, and pass | live N-side rows << 8 (rows: multiple of 16) */
 struct emu_item {
-	int32_t cblock, j0, i0, pass;
+	int32_t cblock, j0, i0, pr;
 };
 
 struct view_meta {
@@ -253,13 +257,15 @@ emu_split_kernel(const xmgd_view_t *__restrict__ views,
 				bits[t][e >> 1] |= h << (16 * (e & 1));
 			}
 		}
-		/* core matrix row: slice t, row r, K octet -> 16 bytes */
+		/* chunk layout [8-row group][slice][2 K core matrices][8 rows x
+		 * 16 B]: the first R rows of a tile are a contiguous prefix, and
+		 * one slice is K-major with SBO = S * 256 B between row groups */
 		const size_t chunk = ((size_t)rt * w.n_ks + ks) * CHUNK_ELEMS;
-		const size_t within = (size_t)((rr >> 3) * 2 + oct) * 64 + (rr & 7) * 8;
+		const size_t within = (size_t)(rr >> 3) * (S * 128) + oct * 64 + (rr & 7) * 8;
 #pragma unroll
 		for (int t = 0; t < S; t++) {
 			uint4 val = make_uint4(bits[t][0], bits[t][1], bits[t][2], bits[t][3]);
-			*reinterpret_cast<uint4 *>(out + chunk + t * (SLICE_BYTES / 2) + within) = val;
+			*reinterpret_cast<uint4 *>(out + chunk + t * 128 + within) = val;
 		}
 	}
 }
@@ -284,8 +290,8 @@ __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 	return min(lim, c0 + EMU_CHUNK);
 }
 
-template <int S, int KEEP, bool LOW, typename TOUT>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
+template <int S, int KEEP, bool LOW, typename TOUT, int DW>
+__global__ void __launch_bounds__(64 + 32 * DW, 1)
 emu_gemm_kernel(const emu_item *__restrict__ items,
     const xmgd_cblock_t *__restrict__ cbs, const xmgd_pair_t *__restrict__ prs,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
@@ -307,6 +313,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 	const emu_item it = items[blockIdx.x];
 	const xmgd_cblock_t cb = cbs[it.cblock];
 	const int F = cbF[it.cblock];
+	const int pass = it.pr & 255, rows = it.pr >> 8;
+	const uint32_t abytes = (uint32_t)rows * S * 32;	/* N-side bytes */
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < NST; s++) {
@@ -314,7 +322,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 			mbar_init(smem_u32(&bar_empty[s]), 1);
 		}
 		mbar_init(smem_u32(&bar_accfull), 1);
-		mbar_init(smem_u32(&bar_accempty), 8);
+		mbar_init(smem_u32(&bar_accempty), DW);
 		mbar_init(smem_u32(&bar_fin), 1);
 		s_err = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -350,13 +358,13 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 					if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1, &s_err, g_err, 1))
 						break;
 					/* imaginary pass: B's re/im halves swapped */
-					const int kb = (cplx && it.pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
+					const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
 					uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 					uint32_t fb = smem_u32(&bar_full[s]);
-					mbar_expect_tx(fb, C::STAGE_BYTES);
+					mbar_expect_tx(fb, C::CHUNK_BYTES + abytes);
 					bulk_g2s(dst, gb + (size_t)kb * C::CHUNK_BYTES, C::CHUNK_BYTES, fb);
 					bulk_g2s(dst + C::CHUNK_BYTES, ga + (size_t)ks * C::CHUNK_BYTES,
-					    C::CHUNK_BYTES, fb);
+					    abytes, fb);
 #pragma unroll
 					for (int q = 0; q < NST; q++)
 						if (q == s)
@@ -382,6 +390,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 		if (lane == 0) {
 			int s = 0, chunk = 0;
 			uint32_t ph = 0, eph = 0;
+			const uint32_t idesc = idesc_n(rows);
 			for (int p = 0; p < cb.npairs && !s_err; p++) {
 				const xmgd_pair_t pr = prs[cb.first_pair + p];
 				const int nks = vb[pr.bview].n_ks;
@@ -411,9 +420,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 								if (pa + qb > KEEP)
 									continue;
 								const int acc = min(pa + qb, 3);
-								uint64_t ad = sdesc(base + qb * SLICE_BYTES);
-								uint64_t bd = sdesc(base + C::CHUNK_BYTES + pa * SLICE_BYTES);
-								mma_bf16(tmem + acc * 128, ad, bd, (started >> acc) & 1u);
+								uint64_t ad = sdesc(base + qb * 256, S * 256);
+								uint64_t bd = sdesc(base + C::CHUNK_BYTES + pa * 256, S * 256);
+								mma_bf16(tmem + acc * 128, ad, bd, idesc,
+								    (started >> acc) & 1u);
 								started |= 1u << acc;
 							}
 						mma_commit(smem_u32(&bar_empty[s]));
@@ -432,12 +442,15 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 				;
 		}
 	} else {
-		/* ---------------- drain + epilogue (warps 2..9) ---------------- */
+		/* ------------- drain + epilogue (warps 2 .. DW+1) -------------
+		 * warp w reads TMEM lanes 32 * (w % 4) .. +31 (the tcgen05.ld
+		 * lane-quadrant rule) and owns NC of the 128 columns */
+		constexpr int NC = 128 / (DW / 4);
 		const int quad = warp & 3, half = (warp - 2) >> 2;
-		const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + half * 64;
-		long long V[64];
+		const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + half * NC;
+		long long V[NC];
 #pragma unroll
-		for (int c = 0; c < 64; c++)
+		for (int c = 0; c < NC; c++)
 			V[c] = 0;
 		uint32_t fph = 0;
 		bool ok = true;
@@ -449,7 +462,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 				/* the pair factor sign * 2^shift (shift 0 or 1, checked by
 				 * the planner) rides on the exact fp32 -> int scales; the
 				 * real pass negates the im * im half */
-				const bool negh = cplx && !it.pass && c0 >= nks / 2;
+				const bool negh = cplx && !pass && c0 >= nks / 2;
 				const float sg = (pr.esign > 0) != negh ? 1.0f : -1.0f;
 				const float s0 = sg * __int_as_float((127 + pr.eshift) << 23);
 				const float s1 = s0 * 256.0f, s2 = s0 * 65536.0f;
@@ -467,16 +480,18 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 				fph ^= 1;
 				tc_fence_after();
 #pragma unroll
-				for (int b8 = 0; b8 < 8; b8++) {
-					float a0[8], a1[8], a2[8], a3[8];
-					tmem_ld8(trow + 0 * 128 + b8 * 8, a0);
-					tmem_ld8(trow + 1 * 128 + b8 * 8, a1);
-					tmem_ld8(trow + 2 * 128 + b8 * 8, a2);
+				for (int b4 = 0; b4 < NC / 4; b4++) {
+					if (half * NC + b4 * 4 >= rows)
+						break;	/* warp-uniform: columns past the tile */
+					float a0[4], a1[4], a2[4], a3[4];
+					tmem_ld4(trow + 0 * 128 + b4 * 4, a0);
+					tmem_ld4(trow + 1 * 128 + b4 * 4, a1);
+					tmem_ld4(trow + 2 * 128 + b4 * 4, a2);
 					if (LOW)
-						tmem_ld8(trow + 3 * 128 + b8 * 8, a3);
+						tmem_ld4(trow + 3 * 128 + b4 * 4, a3);
 					tmem_wait_ld();
 #pragma unroll
-					for (int c = 0; c < 8; c++) {
+					for (int c = 0; c < 4; c++) {
 						/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
 						 * |i0 * 256 + i1| < 2^31 */
 						int i0 = __float2int_rn(a0[c] * s0);
@@ -484,9 +499,18 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 						int i2 = __float2int_rn(a2[c] * s2);
 						long long d = ((long long)(i0 * 256 + i1) << 8) + i2;
 						long long v = d << F;
-						if (LOW)
-							v += __float2ll_rn(a3[c] * s3);
-						V[b8 * 8 + c] += v;
+						if (LOW) {
+							/* low band in units of 2^(-16-F) without a
+							 * 64-bit conversion: x = h * 2^24 + l with
+							 * h = rint(x / 2^24) and l = x - h * 2^24, both
+							 * exact in fp32 and converted as int32 */
+							const float x = a3[c] * s3;
+							const float h = rintf(x * 5.9604644775390625e-8f);
+							const float l = fmaf(h, -16777216.0f, x);
+							v += ((long long)__float2int_rn(h) << 24) +
+							    __float2int_rn(l);
+						}
+						V[b4 * 4 + c] += v;
 					}
 				}
 				tc_fence_before();
@@ -506,12 +530,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 				const bool bz = beta == 0.0;
 				const int cm = cplx ? 2 : 1;
 #pragma unroll
-				for (int c = 0; c < 64; c++) {
-					const int i = it.i0 + half * 64 + c;
+				for (int c = 0; c < NC; c++) {
+					const int i = it.i0 + half * NC + c;
 					if (i < cb.m) {
 						const int e = EA[cb.eA + i] + ej - expoff2 - 16 - F;
 						double v = alpha * ldexp((double)V[c], e);
-						TOUT *cp = Cp + (size_t)cm * (crow[i] + cc) + it.pass;
+						TOUT *cp = Cp + (size_t)cm * (crow[i] + cc) + pass;
 						*cp = bz ? (TOUT)v : (TOUT)fma(beta, (double)*cp, v);
 					}
 				}
@@ -674,20 +698,23 @@ run_emu(xmgd_contract_t *p, const std::vector<int> &cblocks,
 	for (auto &o : order) {
 		const xmgd_cblock_t &cb = p->cblocks[o.second];
 		for (int j0 = 0; j0 < cb.n; j0 += EMU_TM)
-			for (int i0 = 0; i0 < cb.m; i0 += EMU_TM)
+			for (int i0 = 0; i0 < cb.m; i0 += EMU_TM) {
+				/* N-side width: the live rows rounded up to 16 */
+				const int rows = std::min(EMU_TM, (cb.m - i0 + 15) / 16 * 16);
 				for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
-					items.push_back(emu_item{o.second, j0, i0, ps});
+					items.push_back(emu_item{o.second, j0, i0, ps | (rows << 8)});
+			}
 	}
 	if ((st = upload_slot(14, items.data(), items.size() * sizeof(emu_item), &d_items)) ||
 	    (st = upload_slot(15, F.data(), F.size() * sizeof(int32_t), &d_F)))
 		return st;
-	auto kern = emu_gemm_kernel<S, KEEP, LOW, TOUT>;
+	auto kern = emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW>;
 	if (!attr_set) {
 		XMG_CK(cudaFuncSetAttribute(kern,
 		    cudaFuncAttributeMaxDynamicSharedMemorySize, SC::SMEM));
 		attr_set = true;
 	}
-	kern<<<(unsigned)items.size(), GEMM_THREADS, SC::SMEM, stream()>>>(
+	kern<<<(unsigned)items.size(), 64 + 32 * EMU_DW, SC::SMEM, stream()>>>(
 	    (const emu_item *)d_items, d_cbs, d_prs, (const xmgd_view_t *)d_va,
 	    (const xmgd_view_t *)d_vb, d_tabs, EA, EB, (const int32_t *)d_F,
 	    p->alpha[0], p->beta[0], 2 * fin<TIN>::EXPOFF, cplx, (int *)d_err + 1);

@@ -12,10 +12,16 @@ namespace xmg {
 
 constexpr uint64_t WAIT_NS = 2000000000ull;	/* bounded waits: 2 s */
 
-/* tcgen05 instruction descriptor, kind::f16: D f32, A/B bf16, both
- * K-major, N = 128 (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4) */
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
-    ((uint32_t)(128 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+/* tcgen05 instruction descriptor, kind::f16: D f32 (bits 4-5), A and B
+ * bf16 (bits 7-9, 10-12), both K-major, M = 128 (bits 24-28: M >> 4); N
+ * (bits 17-22: N >> 3, a multiple of 16 up to 256) is set per tile */
+constexpr uint32_t IDESC_M128 = (1u << 4) | (1u << 7) | (1u << 10) |
+    ((uint32_t)(128 >> 4) << 24);
+
+__host__ __device__ constexpr uint32_t idesc_n(int n)
+{
+	return IDESC_M128 | ((uint32_t)(n >> 3) << 17);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
@@ -95,20 +101,21 @@ __device__ __forceinline__ void tc_fence_after()
 
 /* shared-memory matrix descriptor: no swizzle, K-major core matrices of
  * 8 rows x 16 bytes; LBO = 128 B between the two K-adjacent core matrices
- * of a 16-wide K step, SBO = 256 B between 8-row groups; bits 46-48 = 1 */
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+ * of a 16-wide K step, SBO = byte distance between 8-row groups; bits
+ * 46-48 = 0b001 (tcgen05 descriptor version) */
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t sbo)
 {
 	return (uint64_t)((saddr & 0x3FFFFu) >> 4) |
-	    ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+	    ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
 	    (1ull << 46);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b,
-    uint32_t acc)
+    uint32_t idesc, uint32_t acc)
 {
 	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
 	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-	    :: "r"(d), "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+	    :: "r"(d), "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar)
@@ -127,6 +134,16 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
 	    : "r"(taddr));
 #pragma unroll
 	for (int i = 0; i < 8; i++)
+		v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4])
+{
+	uint32_t r[4];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
+#pragma unroll
+	for (int i = 0; i < 4; i++)
 		v[i] = __uint_as_float(r[i]);
 }
 
