@@ -123,6 +123,13 @@ int xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b,
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
 
+/* xmg_contract keeps a device plan (metadata, work lists and a CUDA graph
+ * of the launch sequence) for its most recent contractions over GPU-
+ * resident tensors and replays it while the tensors' block tables are
+ * unchanged; XMG_PLAN_CACHE=<n> sets the number kept (0 disables, at most
+ * 16).  This frees every cached plan. */
+void xmg_plan_cache_clear(void);
+
 /* Device-time measurement on the engine's stream: start records an event,
  * stop records another, waits for it and returns the elapsed milliseconds
  * (negative on error). */

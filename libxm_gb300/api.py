@@ -123,6 +123,7 @@ _GB_SIGS = {
     "xmg_contract_flops": (C.c_double, [_P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p]),
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
+    "xmg_plan_cache_clear": (None, []),
     "xm_contract_adjoint": (C.c_int, [Scalar, _P, _P, _P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p]),
     "xmg_timer_start": (C.c_int, []),
     "xmg_timer_stop": (C.c_double, []),

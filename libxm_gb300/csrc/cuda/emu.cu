@@ -96,8 +96,10 @@ template <> struct fin<float> {
 	{ return (int)((__float_as_uint(x) >> 23) & 0xff); }
 };
 
-/* one output tile: block, M-side (B view) row offset, N-side (A view) row
- * offset, and pass | live N-side rows << 8 (rows: multiple of 16) */
+/* one output tile: block, row offsets in b's (j0) and a's (i0) view, and
+ * pr = pass (bit 0) | swap (bit 1) | live N-side rows << 8 (a multiple of
+ * 16).  Without swap b's view is the 128-row M side (TMEM lanes) and a's
+ * the N side (TMEM columns); swap exchanges them. */
 struct emu_item {
 	int32_t cblock, j0, i0, pr;
 };
@@ -292,12 +294,12 @@ __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 
 template <int S, int KEEP, bool LOW, typename TOUT, int DW>
 __global__ void __launch_bounds__(64 + 32 * DW, 1)
-emu_gemm_kernel(const emu_item *__restrict__ items,
+emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
     const xmgd_cblock_t *__restrict__ cbs, const xmgd_pair_t *__restrict__ prs,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ EA,
     const int32_t *__restrict__ EB, const int32_t *__restrict__ cbF,
-    double alpha, double beta, int expoff2, int cplx, int *__restrict__ g_err)
+    double alpha, double beta, int expoff2, int cplx, int *__restrict__ flags)
 {
 	using C = stage_cfg<S>;
 	constexpr int NST = C::NST;
@@ -306,15 +308,17 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 	    (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
 	__shared__ __align__(8) uint64_t bar_full[NST], bar_empty[NST];
 	__shared__ __align__(8) uint64_t bar_accfull, bar_accempty, bar_fin;
+	__shared__ __align__(8) uint64_t bar_ifull[2], bar_iempty[2];
+	__shared__ int s_item[2];
 	__shared__ uint32_t s_tmem;
 	__shared__ volatile int s_err;
+	int *g_err = flags + 1, *g_next = flags + 2;
 
+	/* operands with Inf/NaN (flag set by the exponent kernel): write
+	 * nothing, the host recomputes these blocks on the FP64 path */
+	if (*(volatile int *)flags & 1)
+		return;
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-	const emu_item it = items[blockIdx.x];
-	const xmgd_cblock_t cb = cbs[it.cblock];
-	const int F = cbF[it.cblock];
-	const int pass = it.pr & 255, rows = it.pr >> 8;
-	const uint32_t abytes = (uint32_t)rows * S * 32;	/* N-side bytes */
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < NST; s++) {
@@ -324,6 +328,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 		mbar_init(smem_u32(&bar_accfull), 1);
 		mbar_init(smem_u32(&bar_accempty), DW);
 		mbar_init(smem_u32(&bar_fin), 1);
+		for (int q = 0; q < 2; q++) {
+			mbar_init(smem_u32(&bar_ifull[q]), 1);
+			mbar_init(smem_u32(&bar_iempty[q]), 1 + DW);
+		}
 		s_err = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
@@ -337,6 +345,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 	tc_fence_after();
 	const uint32_t tmem = s_tmem;
 
+	/* persistent: the producer takes the next item of the cost-sorted list
+	 * from a global counter and passes its index to the MMA and drain
+	 * warps through a two-slot ring (-1 ends); the stage ring and the
+	 * accumulator phases carry across items */
 	if (warp == 0) {
 		/* ---------------- producer ---------------- */
 		if (lane == 0) {
@@ -346,30 +358,49 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 #pragma unroll
 			for (int q = 0; q < NST; q++)
 				lastp[q] = -1;
-			for (int p = 0; p < cb.npairs && !s_err; p++) {
-				const xmgd_pair_t pr = prs[cb.first_pair + p];
-				const xmgd_view_t wb = vb[pr.bview], wa = va[pr.aview];
-				const int nks = wb.n_ks, nh = nks / 2;
-				const uint8_t *gb = reinterpret_cast<const uint8_t *>(wb.slices) +
-				    (size_t)(it.j0 / EMU_TM) * nks * C::CHUNK_BYTES;
-				const uint8_t *ga = reinterpret_cast<const uint8_t *>(wa.slices) +
-				    (size_t)(it.i0 / EMU_TM) * nks * C::CHUNK_BYTES;
-				for (int ks = 0; ks < nks; ks++) {
-					if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1, &s_err, g_err, 1))
-						break;
-					/* imaginary pass: B's re/im halves swapped */
-					const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
-					uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
-					uint32_t fb = smem_u32(&bar_full[s]);
-					mbar_expect_tx(fb, C::CHUNK_BYTES + abytes);
-					bulk_g2s(dst, gb + (size_t)kb * C::CHUNK_BYTES, C::CHUNK_BYTES, fb);
-					bulk_g2s(dst + C::CHUNK_BYTES, ga + (size_t)ks * C::CHUNK_BYTES,
-					    abytes, fb);
+			uint32_t iph = 0;
+			for (int slot = 0; !s_err; ) {
+				if (!mbar_wait(smem_u32(&bar_iempty[slot]), iph ^ 1, &s_err, g_err, 5))
+					break;
+				int t = atomicAdd(g_next, 1);
+				t = t < nitems ? t : -1;
+				s_item[slot] = t;
+				mbar_arrive(smem_u32(&bar_ifull[slot]));
+				if (++slot == 2) { slot = 0; iph ^= 1; }
+				if (t < 0)
+					break;
+				const emu_item it = items[t];
+				const xmgd_cblock_t cb = cbs[it.cblock];
+				const int pass = it.pr & 1, swp = (it.pr >> 1) & 1;
+				/* M side: 128 rows; N side: the live rows only */
+				const uint32_t nbytes = (uint32_t)(it.pr >> 8) * S * 32;
+				for (int p = 0; p < cb.npairs && !s_err; p++) {
+					const xmgd_pair_t pr = prs[cb.first_pair + p];
+					const xmgd_view_t wb = vb[pr.bview], wa = va[pr.aview];
+					const int nks = wb.n_ks, nh = nks / 2;
+					const uint8_t *gb = reinterpret_cast<const uint8_t *>(wb.slices) +
+					    (size_t)(it.j0 / EMU_TM) * nks * C::CHUNK_BYTES;
+					const uint8_t *ga = reinterpret_cast<const uint8_t *>(wa.slices) +
+					    (size_t)(it.i0 / EMU_TM) * nks * C::CHUNK_BYTES;
+					const uint8_t *gm = swp ? ga : gb, *gn = swp ? gb : ga;
+					for (int ks = 0; ks < nks; ks++) {
+						if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1, &s_err, g_err, 1))
+							break;
+						/* imaginary pass: B's re/im halves swapped */
+						const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
+						const int km = swp ? ks : kb, kn = swp ? kb : ks;
+						uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
+						uint32_t fb = smem_u32(&bar_full[s]);
+						mbar_expect_tx(fb, C::CHUNK_BYTES + nbytes);
+						bulk_g2s(dst, gm + (size_t)km * C::CHUNK_BYTES, C::CHUNK_BYTES, fb);
+						bulk_g2s(dst + C::CHUNK_BYTES, gn + (size_t)kn * C::CHUNK_BYTES,
+						    nbytes, fb);
 #pragma unroll
-					for (int q = 0; q < NST; q++)
-						if (q == s)
-							lastp[q] = (int)ph;
-					if (++s == NST) { s = 0; ph ^= 1; }
+						for (int q = 0; q < NST; q++)
+							if (q == s)
+								lastp[q] = (int)ph;
+						if (++s == NST) { s = 0; ph ^= 1; }
+					}
 				}
 			}
 			/* on failure, let this CTA's copies still in flight land
@@ -388,50 +419,66 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 	} else if (warp == 1) {
 		/* ---------------- MMA issuer ---------------- */
 		if (lane == 0) {
-			int s = 0, chunk = 0;
+			int s = 0;
+			bool first = true;
 			uint32_t ph = 0, eph = 0;
-			const uint32_t idesc = idesc_n(rows);
-			for (int p = 0; p < cb.npairs && !s_err; p++) {
-				const xmgd_pair_t pr = prs[cb.first_pair + p];
-				const int nks = vb[pr.bview].n_ks;
-				for (int c0 = 0; c0 < nks && !s_err; ) {
-					const int c1 = chunk_end(c0, nks, cplx);
-					if (chunk > 0) {
-						if (!mbar_wait(smem_u32(&bar_accempty), eph, &s_err, g_err, 2))
-							break;
-						eph ^= 1;
-					}
-					tc_fence_after();
-					/* every accumulator restarts each chunk: the exact
-					 * groups for their 2^23 bound, the low band because the
-					 * tensor core's fp32 accumulation error grows with the
-					 * accumulation length (per-pair accumulation measured
-					 * 10x larger error) */
-					uint32_t started = 0;
-					for (int ks = c0; ks < c1; ks++) {
-						if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3))
-							break;
+			uint32_t iph = 0;
+			for (int slot = 0; !s_err; ) {
+				if (!mbar_wait(smem_u32(&bar_ifull[slot]), iph, &s_err, g_err, 6))
+					break;
+				const int t = s_item[slot];
+				mbar_arrive(smem_u32(&bar_iempty[slot]));
+				if (++slot == 2) { slot = 0; iph ^= 1; }
+				if (t < 0)
+					break;
+				const emu_item it = items[t];
+				const xmgd_cblock_t cb = cbs[it.cblock];
+				const uint32_t idesc = idesc_n(it.pr >> 8);
+				for (int p = 0; p < cb.npairs && !s_err; p++) {
+					const xmgd_pair_t pr = prs[cb.first_pair + p];
+					const int nks = vb[pr.bview].n_ks;
+					for (int c0 = 0; c0 < nks && !s_err; ) {
+						const int c1 = chunk_end(c0, nks, cplx);
+						/* the accumulators are free once the drain warps
+						 * have read the previous chunk (of this or the
+						 * previous item) */
+						if (!first) {
+							if (!mbar_wait(smem_u32(&bar_accempty), eph, &s_err, g_err, 2))
+								break;
+							eph ^= 1;
+						}
+						first = false;
 						tc_fence_after();
-						const uint32_t base = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
+						/* every accumulator restarts each chunk: the exact
+						 * groups for their 2^23 bound, the low band because
+						 * the tensor core's fp32 accumulation error grows
+						 * with the accumulation length (per-pair
+						 * accumulation measured 10x larger error) */
+						uint32_t started = 0;
+						for (int ks = c0; ks < c1; ks++) {
+							if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3))
+								break;
+							tc_fence_after();
+							const uint32_t base = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 #pragma unroll
-						for (int pa = 0; pa < S; pa++)
+							for (int pa = 0; pa < S; pa++)
 #pragma unroll
-							for (int qb = 0; qb < S; qb++) {
-								if (pa + qb > KEEP)
-									continue;
-								const int acc = min(pa + qb, 3);
-								uint64_t ad = sdesc(base + qb * 256, S * 256);
-								uint64_t bd = sdesc(base + C::CHUNK_BYTES + pa * 256, S * 256);
-								mma_bf16(tmem + acc * 128, ad, bd, idesc,
-								    (started >> acc) & 1u);
-								started |= 1u << acc;
-							}
-						mma_commit(smem_u32(&bar_empty[s]));
-						if (++s == NST) { s = 0; ph ^= 1; }
+								for (int qb = 0; qb < S; qb++) {
+									if (pa + qb > KEEP)
+										continue;
+									const int acc = min(pa + qb, 3);
+									uint64_t ad = sdesc(base + qb * 256, S * 256);
+									uint64_t bd = sdesc(base + C::CHUNK_BYTES + pa * 256, S * 256);
+									mma_bf16(tmem + acc * 128, ad, bd, idesc,
+									    (started >> acc) & 1u);
+									started |= 1u << acc;
+								}
+							mma_commit(smem_u32(&bar_empty[s]));
+							if (++s == NST) { s = 0; ph ^= 1; }
+						}
+						mma_commit(smem_u32(&bar_accfull));
+						c0 = c1;
 					}
-					mma_commit(smem_u32(&bar_accfull));
-					chunk++;
-					c0 = c1;
 				}
 			}
 			/* every MMA issued by this CTA has completed once bar_fin
@@ -448,101 +495,126 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 		constexpr int NC = 128 / (DW / 4);
 		const int quad = warp & 3, half = (warp - 2) >> 2;
 		const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + half * NC;
-		long long V[NC];
-#pragma unroll
-		for (int c = 0; c < NC; c++)
-			V[c] = 0;
 		uint32_t fph = 0;
 		bool ok = true;
-		for (int p = 0; p < cb.npairs && ok; p++) {
-			const xmgd_pair_t pr = prs[cb.first_pair + p];
-			const int nks = vb[pr.bview].n_ks;
-			for (int c0 = 0; c0 < nks; ) {
-				const int c1 = chunk_end(c0, nks, cplx);
-				/* the pair factor sign * 2^shift (shift 0 or 1, checked by
-				 * the planner) rides on the exact fp32 -> int scales; the
-				 * real pass negates the im * im half */
-				const bool negh = cplx && !pass && c0 >= nks / 2;
-				const float sg = (pr.esign > 0) != negh ? 1.0f : -1.0f;
-				const float s0 = sg * __int_as_float((127 + pr.eshift) << 23);
-				const float s1 = s0 * 256.0f, s2 = s0 * 65536.0f;
-				const float s3 = s0 * __int_as_float((127 + 16 + F) << 23);
-				/* one lane waits, the warp follows its verdict, so the
-				 * .sync.aligned TMEM loads below stay convergent */
-				int w = 1;
-				if (lane == 0)
-					w = mbar_wait(smem_u32(&bar_accfull), fph, &s_err, g_err, 4);
-				w = __shfl_sync(0xffffffffu, w, 0);
-				if (!w) {
-					ok = false;
-					break;
-				}
-				fph ^= 1;
-				tc_fence_after();
-#pragma unroll
-				for (int b4 = 0; b4 < NC / 4; b4++) {
-					if (half * NC + b4 * 4 >= rows)
-						break;	/* warp-uniform: columns past the tile */
-					float a0[4], a1[4], a2[4], a3[4];
-					tmem_ld4(trow + 0 * 128 + b4 * 4, a0);
-					tmem_ld4(trow + 1 * 128 + b4 * 4, a1);
-					tmem_ld4(trow + 2 * 128 + b4 * 4, a2);
-					if (LOW)
-						tmem_ld4(trow + 3 * 128 + b4 * 4, a3);
-					tmem_wait_ld();
-#pragma unroll
-					for (int c = 0; c < 4; c++) {
-						/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
-						 * |i0 * 256 + i1| < 2^31 */
-						int i0 = __float2int_rn(a0[c] * s0);
-						int i1 = __float2int_rn(a1[c] * s1);
-						int i2 = __float2int_rn(a2[c] * s2);
-						long long d = ((long long)(i0 * 256 + i1) << 8) + i2;
-						long long v = d << F;
-						if (LOW) {
-							/* low band in units of 2^(-16-F) without a
-							 * 64-bit conversion: x = h * 2^24 + l with
-							 * h = rint(x / 2^24) and l = x - h * 2^24, both
-							 * exact in fp32 and converted as int32 */
-							const float x = a3[c] * s3;
-							const float h = rintf(x * 5.9604644775390625e-8f);
-							const float l = fmaf(h, -16777216.0f, x);
-							v += ((long long)__float2int_rn(h) << 24) +
-							    __float2int_rn(l);
-						}
-						V[b4 * 4 + c] += v;
-					}
-				}
-				tc_fence_before();
-				__syncwarp();
-				if (lane == 0)
-					mbar_arrive(smem_u32(&bar_accempty));
-				c0 = c1;
+		uint32_t iph = 0;
+		for (int slot = 0; ok; ) {
+			int t = -1;
+			if (lane == 0) {
+				if (mbar_wait(smem_u32(&bar_ifull[slot]), iph, &s_err, g_err, 7)) {
+					t = s_item[slot];
+					mbar_arrive(smem_u32(&bar_iempty[slot]));
+				} else
+					t = -2;
 			}
-		}
-		if (ok && !s_err) {
-			const int j = it.j0 + quad * 32 + lane;
-			if (j < cb.n) {
+			t = __shfl_sync(0xffffffffu, t, 0);
+			if (++slot == 2) { slot = 0; iph ^= 1; }
+			if (t < 0)
+				break;
+			const emu_item it = items[t];
+			const xmgd_cblock_t cb = cbs[it.cblock];
+			const int F = cbF[it.cblock];
+			const int pass = it.pr & 1, swp = (it.pr >> 1) & 1, rows = it.pr >> 8;
+			long long V[NC];
+#pragma unroll
+			for (int c = 0; c < NC; c++)
+				V[c] = 0;
+			for (int p = 0; p < cb.npairs && ok; p++) {
+				const xmgd_pair_t pr = prs[cb.first_pair + p];
+				const int nks = vb[pr.bview].n_ks;
+				for (int c0 = 0; c0 < nks; ) {
+					const int c1 = chunk_end(c0, nks, cplx);
+					/* the pair factor sign * 2^shift (shift 0 or 1, checked
+					 * by the planner) rides on the exact fp32 -> int
+					 * scales; the real pass negates the im * im half */
+					const bool negh = cplx && !pass && c0 >= nks / 2;
+					const float sg = (pr.esign > 0) != negh ? 1.0f : -1.0f;
+					const float s0 = sg * __int_as_float((127 + pr.eshift) << 23);
+					const float s1 = s0 * 256.0f, s2 = s0 * 65536.0f;
+					const float s3 = s0 * __int_as_float((127 + 16 + F) << 23);
+					/* one lane waits, the warp follows its verdict, so the
+					 * .sync.aligned TMEM loads below stay convergent */
+					int w = 1;
+					if (lane == 0)
+						w = mbar_wait(smem_u32(&bar_accfull), fph, &s_err, g_err, 4);
+					w = __shfl_sync(0xffffffffu, w, 0);
+					if (!w) {
+						ok = false;
+						break;
+					}
+					fph ^= 1;
+					tc_fence_after();
+#pragma unroll
+					for (int b4 = 0; b4 < NC / 4; b4++) {
+						if (half * NC + b4 * 4 >= rows)
+							break;	/* warp-uniform: columns past the tile */
+						float a0[4], a1[4], a2[4], a3[4];
+						tmem_ld4(trow + 0 * 128 + b4 * 4, a0);
+						tmem_ld4(trow + 1 * 128 + b4 * 4, a1);
+						tmem_ld4(trow + 2 * 128 + b4 * 4, a2);
+						if (LOW)
+							tmem_ld4(trow + 3 * 128 + b4 * 4, a3);
+						tmem_wait_ld();
+#pragma unroll
+						for (int c = 0; c < 4; c++) {
+							/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
+							 * |i0 * 256 + i1| < 2^31 */
+							int i0 = __float2int_rn(a0[c] * s0);
+							int i1 = __float2int_rn(a1[c] * s1);
+							int i2 = __float2int_rn(a2[c] * s2);
+							long long d = ((long long)(i0 * 256 + i1) << 8) + i2;
+							long long v = d << F;
+							if (LOW) {
+								/* low band in units of 2^(-16-F) without a
+								 * 64-bit conversion: x = h * 2^24 + l with
+								 * h = rint(x / 2^24) and l = x - h * 2^24,
+								 * both exact in fp32 and converted as int32 */
+								const float x = a3[c] * s3;
+								const float h = rintf(x * 5.9604644775390625e-8f);
+								const float l = fmaf(h, -16777216.0f, x);
+								v += ((long long)__float2int_rn(h) << 24) +
+								    __float2int_rn(l);
+							}
+							V[b4 * 4 + c] += v;
+						}
+					}
+					tc_fence_before();
+					__syncwarp();
+					if (lane == 0)
+						mbar_arrive(smem_u32(&bar_accempty));
+					c0 = c1;
+				}
+			}
+			if (!ok || s_err)
+				break;
+			/* epilogue (overlaps the next item's first chunk of MMAs):
+			 * this thread's TMEM lane is one M-side row; its columns are
+			 * N-side rows.  Without swap the M side is b's free index (j),
+			 * with swap a's (i). */
+			const int ms = (swp ? it.i0 : it.j0) + quad * 32 + lane;
+			const int q0 = (swp ? it.j0 : it.i0) + half * NC;
+			const int flim = swp ? cb.m : cb.n, vlim = swp ? cb.n : cb.m;
+			if (ms < flim) {
 				TOUT *Cp = reinterpret_cast<TOUT *>(cb.c_ptr);
-				const int32_t *crow = tabs + cb.crow;
-				const int32_t cc = tabs[cb.ccol + j];
-				const int ej = EB[cb.eB + j];
+				const int32_t *vtab = tabs + (swp ? cb.ccol : cb.crow);
+				const int32_t *vexp = swp ? EB + cb.eB : EA + cb.eA;
+				const int32_t fo = tabs[(swp ? cb.crow : cb.ccol) + ms];
+				const int fe = (swp ? EA + cb.eA : EB + cb.eB)[ms];
 				const bool bz = beta == 0.0;
 				const int cm = cplx ? 2 : 1;
 #pragma unroll
 				for (int c = 0; c < NC; c++) {
-					const int i = it.i0 + half * NC + c;
-					if (i < cb.m) {
-						const int e = EA[cb.eA + i] + ej - expoff2 - 16 - F;
+					const int q = q0 + c;
+					if (q < vlim) {
+						const int e = vexp[q] + fe - expoff2 - 16 - F;
 						double v = alpha * ldexp((double)V[c], e);
-						TOUT *cp = Cp + (size_t)cm * (crow[i] + cc) + pass;
+						TOUT *cp = Cp + (size_t)cm * (vtab[q] + fo) + pass;
 						*cp = bz ? (TOUT)v : (TOUT)fma(beta, (double)*cp, v);
 					}
 				}
 			}
 		}
 	}
-
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
@@ -552,56 +624,291 @@ emu_gemm_kernel(const emu_item *__restrict__ items,
 }
 
 /* ------------------------------------------------------------------ */
-/* host orchestration                                                  */
+/* host side: a reusable plan with an online tile-orientation autotuner  */
 
-static int
-upload_slot(int slot, const void *h, size_t bytes, uint64_t *d)
+/*
+ * Tile orientation per output block.  The M side of a tile is always 128
+ * rows (TMEM lanes); the N side is the live rows rounded up to 16, so the
+ * choice of which operand lies on the N side sets the padded work.  Three
+ * policies, each a complete work list:
+ *   0  per block, the orientation with less padded MMA work;
+ *   1  a on the N side everywhere;
+ *   2  per block, the cheaper orientation under a shared-memory model of
+ *      one K step, max(N / 2, 32 + N / 4) cycles: the M-side operand
+ *      (4 KiB) and the N-side operand (N * 32 B) are read from shared
+ *      memory at 128 B per cycle while the tensor core needs N / 2 cycles.
+ * The first runs of a plan replay each distinct policy once, timed with
+ * events, then keep the fastest; the choice is remembered per block-size
+ * histogram so later plans of the same shape start tuned.
+ */
+enum { EMU_NPOLICY = 3 };
+
+static double
+tile_cost(int mside, int nside, int policy)
 {
-	int st;
+	double c = 0;
+	const int mt = (mside + EMU_TM - 1) / EMU_TM;
+	for (int n0 = 0; n0 < nside; n0 += EMU_TM) {
+		const int w = std::min(EMU_TM, (nside - n0 + 15) / 16 * 16);
+		c += policy == 2 ? std::max(w / 2.0, 32.0 + w / 4.0) : (double)w;
+	}
+	return c * mt;
+}
 
-	if ((st = xmgd_scratch(slot, bytes ? bytes : 16, d)) != XMG_OK)
-		return st;
-	if (bytes)
-		return check(cudaMemcpyAsync((void *)*d, h, bytes,
-		    cudaMemcpyHostToDevice, stream()), "emu upload");
+static uint64_t
+mix64(uint64_t h)
+{
+	h ^= h >> 33; h *= 0xff51afd7ed558ccdULL;
+	h ^= h >> 33; h *= 0xc4ceb93fe53e6ccdULL;
+	return h ^ (h >> 33);
+}
+
+struct tune_entry {
+	uint64_t sig;
+	int policy;
+};
+static std::vector<tune_entry> g_tuned;
+
+struct emu_cand {
+	int policy;
+	uint64_t d_items;
+	int nitems, grid;
+	float ms;
+};
+
+struct emu_plan {
+	int dtype, cplx;
+	double alpha, beta;
+	std::vector<xmgd_view_t> VA, VB;     /* slices: offsets in the workspace */
+	std::vector<char> useA, useB;
+	uint64_t d_va = 0, d_vb = 0, d_meta[2][2] = {{0, 0}, {0, 0}};
+	int64_t nctas[2][2] = {{0, 0}, {0, 0}};
+	uint64_t d_E = 0, d_F = 0;
+	int64_t nE = 0;
+	int32_t nexp_a = 0;
+	size_t slice_bytes = 0;
+	uint64_t ws = 0;                     /* workspace the views point into */
+	const xmgd_cblock_t *d_cbs;
+	const xmgd_pair_t *d_prs;
+	const int32_t *d_tabs;
+	std::vector<emu_cand> cand;
+	int cur = 0, tuned = 0;
+	uint64_t sig = 0;
+	int *h_flags = nullptr;              /* pinned: Inf/NaN, timeout */
+	int (*split)(emu_plan *) = nullptr;
+	int (*gemm)(emu_plan *) = nullptr;
+};
+
+/* exponent tables, then unfold + split of every used view of both sides */
+template <typename TIN>
+static int
+launch_split(emu_plan *e)
+{
+	int32_t *EA = (int32_t *)e->d_E, *EB = EA + e->nexp_a;
+	int *flags = (int *)(EA + e->nE);
+
+	XMG_CK(cudaMemsetAsync((void *)e->d_E, 0, (e->nE + 64) * sizeof(int32_t),
+	    stream()));
+	for (int side = 0; side < 2; side++) {
+		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
+		const int nv = (int)(side ? e->VB.size() : e->VA.size());
+		int32_t *E = side ? EB : EA;
+		if (e->nctas[side][0] > 0) {
+			emu_exp_kernel<TIN><<<(unsigned)e->nctas[side][0], 256, 0, stream()>>>(
+			    dv, (const view_meta *)e->d_meta[side][0], nv, e->d_tabs, E, flags);
+			g_launches++;
+			XMG_CK(cudaGetLastError());
+		}
+	}
+	for (int side = 0; side < 2; side++) {
+		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
+		const int nv = (int)(side ? e->VB.size() : e->VA.size());
+		const int32_t *E = side ? EB : EA;
+		if (e->nctas[side][1] > 0) {
+			emu_split_kernel<TIN><<<(unsigned)e->nctas[side][1], 256, 0, stream()>>>(
+			    dv, (const view_meta *)e->d_meta[side][1], nv, e->d_tabs, E);
+			g_launches++;
+			XMG_CK(cudaGetLastError());
+		}
+	}
+	return XMG_OK;
+}
+
+/* the persistent grouped GEMM of the current candidate, then the flags */
+template <typename TIN, typename TOUT>
+static int
+launch_gemm(emu_plan *e)
+{
+	constexpr int S = fin<TIN>::S, KEEP = fin<TIN>::KEEP;
+	constexpr bool LOW = KEEP > 2;
+	const emu_cand &c = e->cand[e->cur];
+	int32_t *EA = (int32_t *)e->d_E, *EB = EA + e->nexp_a;
+	int *flags = (int *)(EA + e->nE);
+
+	emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW><<<(unsigned)c.grid,
+	    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
+	    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
+	    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
+	    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
+	    2 * fin<TIN>::EXPOFF, e->cplx, flags);
+	g_launches++;
+	XMG_CK(cudaGetLastError());
+	XMG_CK(cudaMemcpyAsync(e->h_flags, flags, 2 * sizeof(int),
+	    cudaMemcpyDeviceToHost, stream()));
 	return XMG_OK;
 }
 
 template <typename TIN, typename TOUT>
 static int
-run_emu(xmgd_contract_t *p, const std::vector<int> &cblocks,
-    const xmgd_cblock_t *d_cbs, const xmgd_pair_t *d_prs,
-    const int32_t *d_tabs, xmgd_timing_t *tm, int cplx)
+set_attrs()
 {
 	constexpr int S = fin<TIN>::S, KEEP = fin<TIN>::KEEP;
-	constexpr bool LOW = KEEP > 2;
-	using SC = stage_cfg<S>;
-	static bool attr_set = false;
-	std::vector<xmgd_view_t> VA(p->views_a, p->views_a + p->nviews_a);
-	std::vector<xmgd_view_t> VB(p->views_b, p->views_b + p->nviews_b);
-	std::vector<char> useA(VA.size(), 0), useB(VB.size(), 0);
-	std::vector<int32_t> F(p->ncblocks, 0);
-	std::vector<emu_item> items;
-	uint64_t d_slices, d_E, d_va, d_vb, d_items, d_F, d_meta, d_err;
+	static bool done = false;
+	if (!done) {
+		XMG_CK(cudaFuncSetAttribute(emu_gemm_kernel<S, KEEP, (KEEP > 2), TOUT, EMU_DW>,
+		    cudaFuncAttributeMaxDynamicSharedMemorySize, stage_cfg<S>::SMEM));
+		done = true;
+	}
+	return XMG_OK;
+}
+
+static int
+upload_new(const void *h, size_t bytes, uint64_t *d)
+{
 	int st;
 
+	if ((st = xmgd_alloc(bytes ? bytes : 16, d)) != XMG_OK)
+		return st;
+	if (bytes)
+		XMG_CK(cudaMemcpyAsync((void *)*d, h, bytes, cudaMemcpyHostToDevice,
+		    stream()));
+	return XMG_OK;
+}
+
+void
+emu_free(emu_plan *e)
+{
+	if (!e)
+		return;
+	uint64_t bufs[] = {e->d_va, e->d_vb, e->d_meta[0][0], e->d_meta[0][1],
+	    e->d_meta[1][0], e->d_meta[1][1], e->d_E, e->d_F};
+	for (uint64_t b : bufs)
+		if (b)
+			xmgd_free(b);
+	for (emu_cand &c : e->cand)
+		if (c.d_items)
+			xmgd_free(c.d_items);
+	if (e->h_flags)
+		cudaFreeHost(e->h_flags);
+	delete e;
+}
+
+/* work list of one policy: blocks by decreasing cost, tiles adjacent */
+static void
+make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
+    int policy, std::vector<emu_item> &items)
+{
+	std::vector<std::pair<double, int>> order;
+	for (int ci : cblocks) {
+		const xmgd_cblock_t &cb = p->cblocks[ci];
+		double c = 0;
+		for (int q = 0; q < cb.npairs; q++)
+			c += p->pairs[cb.first_pair + q].k;
+		order.push_back({-c * cb.m * (double)cb.n, ci});
+	}
+	std::stable_sort(order.begin(), order.end());
+	items.clear();
+	for (auto &o : order) {
+		const xmgd_cblock_t &cb = p->cblocks[o.second];
+		bool swp = false;
+		if (policy != 1) {
+			const int pol = policy == 2 ? 2 : 0;
+			swp = tile_cost(cb.m, cb.n, pol) < tile_cost(cb.n, cb.m, pol);
+		}
+		const int mlen = swp ? cb.m : cb.n, nlen = swp ? cb.n : cb.m;
+		for (int m0 = 0; m0 < mlen; m0 += EMU_TM)
+			for (int n0 = 0; n0 < nlen; n0 += EMU_TM) {
+				const int rows = std::min(EMU_TM, (nlen - n0 + 15) / 16 * 16);
+				const int i0 = swp ? m0 : n0, j0 = swp ? n0 : m0;
+				for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
+					items.push_back(emu_item{o.second, j0, i0,
+					    ps | (swp ? 2 : 0) | (rows << 8)});
+			}
+	}
+}
+
+int
+emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
+    const xmgd_cblock_t *d_cbs, const xmgd_pair_t *d_prs,
+    const int32_t *d_tabs, emu_plan **out)
+{
+	const bool realab = p->alpha[1] == 0 && p->beta[1] == 0;
+	int cplx, st;
+
+	*out = nullptr;
+	switch (p->dtype) {
+	case 0: case 2: cplx = 0; break;
+	case 1: case 3:
+		/* two real passes need real alpha and beta */
+		if (!realab)
+			return xmg_seterr(XMG_ENOTSUP, "split-precision path: complex "
+			    "alpha/beta");
+		cplx = 1;
+		break;
+	default:
+		return xmg_seterr(XMG_ENOTSUP, "split-precision path: scalar type");
+	}
+	const bool dbl = p->dtype >= 2;
+	const int chunk_bytes = (dbl ? fin<double>::S : fin<float>::S) * SLICE_BYTES;
+	emu_plan *e = new emu_plan();
+	e->dtype = p->dtype;
+	e->cplx = cplx;
+	e->alpha = p->alpha[0];
+	e->beta = p->beta[0];
+	e->d_cbs = d_cbs;
+	e->d_prs = d_prs;
+	e->d_tabs = d_tabs;
+	e->VA.assign(p->views_a, p->views_a + p->nviews_a);
+	e->VB.assign(p->views_b, p->views_b + p->nviews_b);
+	e->useA.assign(e->VA.size(), 0);
+	e->useB.assign(e->VB.size(), 0);
+	e->split = dbl ? launch_split<double> : launch_split<float>;
+	e->gemm = dbl ? launch_gemm<double, double> : launch_gemm<float, float>;
+	if ((st = dbl ? set_attrs<double, double>() : set_attrs<float, float>()))
+		goto fail;
+
+	{
 	/* operand views used by the emulated blocks, and the fixed-point
 	 * scale F of every block (|V| <= K_eff * 2^(30+F) < 2^61) */
+	std::vector<int32_t> F(p->ncblocks, 0);
+	std::vector<uint64_t> hist;
 	for (int ci : cblocks) {
 		const xmgd_cblock_t &cb = p->cblocks[ci];
 		double keff = 0;
+		int64_t ksum = 0;
 		for (int q = 0; q < cb.npairs; q++) {
 			const xmgd_pair_t &pr = p->pairs[cb.first_pair + q];
-			useA[pr.aview] = useB[pr.bview] = 1;
+			e->useA[pr.aview] = e->useB[pr.bview] = 1;
 			double kr = cplx ? 2.0 * 16 * ((pr.k + 15) / 16) : pr.k;
 			keff += ldexp(1.0, std::max(pr.eshift, 0)) * kr;
+			ksum += pr.k;
 		}
 		int lg = (int)ceil(log2(std::max(keff, 2.0)));
-		if (lg > 31)
-			return xmg_seterr(XMG_ENOTSUP, "split-precision path: K too large");
+		if (lg > 31) {
+			st = xmg_seterr(XMG_ENOTSUP, "split-precision path: K too large");
+			goto fail;
+		}
 		F[ci] = std::min(24, 31 - lg);
+		hist.push_back(mix64(((uint64_t)cb.m << 40) ^ ((uint64_t)cb.n << 20) ^
+		    (uint64_t)ksum));
 	}
-	/* slice storage */
+	std::sort(hist.begin(), hist.end());
+	uint64_t sig = mix64((uint64_t)p->dtype + 1);
+	for (uint64_t h : hist)
+		sig = mix64(sig ^ h);
+	e->sig = sig;
+
+	/* slice storage: offsets now, rebased onto the workspace at bind */
 	size_t off = 0;
 	auto tile = [&](std::vector<xmgd_view_t> &V, std::vector<char> &use) {
 		for (size_t v = 0; v < V.size(); v++) {
@@ -614,41 +921,17 @@ run_emu(xmgd_contract_t *p, const std::vector<int> &cblocks,
 			w.n_ks = (cplx ? 2 : 1) * (w.khp / EMU_KS);
 			w.kfast = w.k > 1 && p->tabs[w.rowtab + 1] - p->tabs[w.rowtab] == 1;
 			w.slices = off;
-			off += (size_t)w.n_rt * w.n_ks * SC::CHUNK_BYTES;
+			off += (size_t)w.n_rt * w.n_ks * chunk_bytes;
 		}
 	};
-	tile(VA, useA);
-	tile(VB, useB);
-	if ((st = xmgd_scratch(8, off, &d_slices)) != XMG_OK)
-		return st;
-	for (size_t v = 0; v < VA.size(); v++)
-		if (useA[v]) VA[v].slices += d_slices;
-	for (size_t v = 0; v < VB.size(); v++)
-		if (useB[v]) VB[v].slices += d_slices;
-	tm->slice_bytes = (int64_t)off;
+	tile(e->VA, e->useA);
+	tile(e->VB, e->useB);
+	e->slice_bytes = off;
 
-	size_t nE = (size_t)p->nexp_a + p->nexp_b;
-	if ((st = xmgd_scratch(9, (nE + 64) * sizeof(int32_t), &d_E)) != XMG_OK)
-		return st;
-	XMG_CK(cudaMemsetAsync((void *)d_E, 0, (nE + 64) * sizeof(int32_t), stream()));
-	int32_t *EA = (int32_t *)d_E, *EB = EA + p->nexp_a;
-	d_err = (uint64_t)(EB + p->nexp_b);	/* flags live after the tables */
-	if ((st = upload_slot(10, VA.data(), VA.size() * sizeof(xmgd_view_t), &d_va)) ||
-	    (st = upload_slot(11, VB.data(), VB.size() * sizeof(xmgd_view_t), &d_vb)))
-		return st;
-
-	cudaEvent_t e0, e1, e2;
-	XMG_CK(cudaEventCreate(&e0));
-	XMG_CK(cudaEventCreate(&e1));
-	XMG_CK(cudaEventCreate(&e2));
-	XMG_CK(cudaEventRecord(e0, stream()));
-
-	/* exponent and split launches over the used views of each side */
+	/* CTA ranges of the exponent and split launches of each side */
 	for (int side = 0; side < 2; side++) {
-		std::vector<xmgd_view_t> &V = side ? VB : VA;
-		std::vector<char> &use = side ? useB : useA;
-		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? d_vb : d_va);
-		int32_t *E = side ? EB : EA;
+		std::vector<xmgd_view_t> &V = side ? e->VB : e->VA;
+		std::vector<char> &use = side ? e->useB : e->useA;
 		for (int kind = 0; kind < 2; kind++) {
 			std::vector<view_meta> meta(V.size());
 			int64_t n = 0;
@@ -661,107 +944,125 @@ run_emu(xmgd_contract_t *p, const std::vector<int> &cblocks,
 				else
 					n += (int64_t)V[v].n_rt * ((V[v].n_ks + 3) / 4);
 			}
-			if (n == 0)
-				continue;
-			if ((st = upload_slot(12 + kind, meta.data(), meta.size() *
-			    sizeof(view_meta), &d_meta)))
-				return st;
-			if (kind == 0)
-				emu_exp_kernel<TIN><<<(unsigned)n, 256, 0, stream()>>>(dv,
-				    (const view_meta *)d_meta, (int)V.size(), d_tabs, E,
-				    (int *)d_err);
-			else
-				emu_split_kernel<TIN><<<(unsigned)n, 256, 0, stream()>>>(dv,
-				    (const view_meta *)d_meta, (int)V.size(), d_tabs, E);
-			g_launches++;
-			XMG_CK(cudaGetLastError());
-			/* the meta buffer is reused by the next launch */
-			XMG_CK(cudaStreamSynchronize(stream()));
+			e->nctas[side][kind] = n;
+			if ((st = upload_new(meta.data(), meta.size() * sizeof(view_meta),
+			    &e->d_meta[side][kind])))
+				goto fail;
 		}
 	}
-	int flags[2] = {0, 0};
-	XMG_CK(cudaMemcpy(flags, (void *)d_err, sizeof flags, cudaMemcpyDeviceToHost));
-	if (flags[0] & 1)
-		return xmg_seterr(XMG_ENOTSUP, "split-precision path: Inf/NaN in operands");
-	XMG_CK(cudaEventRecord(e1, stream()));
+	e->nexp_a = p->nexp_a;
+	e->nE = (int64_t)p->nexp_a + p->nexp_b;
+	if ((st = xmgd_alloc((e->nE + 64) * sizeof(int32_t), &e->d_E)) ||
+	    (st = upload_new(F.data(), F.size() * sizeof(int32_t), &e->d_F)) ||
+	    (st = xmgd_alloc(e->VA.size() * sizeof(xmgd_view_t) + 16, &e->d_va)) ||
+	    (st = xmgd_alloc(e->VB.size() * sizeof(xmgd_view_t) + 16, &e->d_vb)))
+		goto fail;
 
-	/* work list: output blocks by decreasing cost, tiles adjacent */
-	std::vector<std::pair<double, int>> order;
-	for (int ci : cblocks) {
-		const xmgd_cblock_t &cb = p->cblocks[ci];
-		double c = 0;
-		for (int q = 0; q < cb.npairs; q++)
-			c += p->pairs[cb.first_pair + q].k;
-		order.push_back({-c * cb.m * (double)cb.n, ci});
+	/* work lists: a remembered policy for this histogram, else every
+	 * distinct policy once */
+	int known = -1;
+	for (const tune_entry &t : g_tuned)
+		if (t.sig == sig)
+			known = t.policy;
+	if (getenv("XMG_TUNE") && strcmp(getenv("XMG_TUNE"), "0") == 0)
+		known = 0;
+	std::vector<std::vector<emu_item>> lists;
+	for (int pol = 0; pol < EMU_NPOLICY; pol++) {
+		if (known >= 0 && pol != known)
+			continue;
+		std::vector<emu_item> items;
+		make_items(p, cblocks, cplx, pol, items);
+		bool dup = false;
+		for (auto &l : lists)
+			dup |= l.size() == items.size() && memcmp(l.data(), items.data(),
+			    items.size() * sizeof(emu_item)) == 0;
+		if (dup)
+			continue;
+		emu_cand c;
+		c.policy = pol;
+		c.nitems = (int)items.size();
+		c.grid = std::min(c.nitems, num_sms());
+		c.ms = -1;
+		if ((st = upload_new(items.data(), items.size() * sizeof(emu_item),
+		    &c.d_items)))
+			goto fail;
+		e->cand.push_back(c);
+		lists.push_back(std::move(items));
 	}
-	std::stable_sort(order.begin(), order.end());
-	for (auto &o : order) {
-		const xmgd_cblock_t &cb = p->cblocks[o.second];
-		for (int j0 = 0; j0 < cb.n; j0 += EMU_TM)
-			for (int i0 = 0; i0 < cb.m; i0 += EMU_TM) {
-				/* N-side width: the live rows rounded up to 16 */
-				const int rows = std::min(EMU_TM, (cb.m - i0 + 15) / 16 * 16);
-				for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
-					items.push_back(emu_item{o.second, j0, i0, ps | (rows << 8)});
-			}
+	e->tuned = e->cand.size() <= 1;
+	if ((st = check(cudaMallocHost(&e->h_flags, 2 * sizeof(int)), "flags")) ||
+	    (st = check(cudaStreamSynchronize(stream()), "plan upload")))
+		goto fail;
+	e->h_flags[0] = e->h_flags[1] = 0;
 	}
-	if ((st = upload_slot(14, items.data(), items.size() * sizeof(emu_item), &d_items)) ||
-	    (st = upload_slot(15, F.data(), F.size() * sizeof(int32_t), &d_F)))
+	*out = e;
+	return XMG_OK;
+fail:
+	emu_free(e);
+	return st;
+}
+
+/* Slice workspace and absolute view addresses; *moved when the views had
+ * to be re-uploaded (a captured graph holding the old ones is stale). */
+int
+emu_bind(emu_plan *e, bool *moved)
+{
+	uint64_t ws;
+	int st;
+
+	*moved = false;
+	if ((st = xmgd_scratch(8, e->slice_bytes + 16, &ws)) != XMG_OK)
 		return st;
-	auto kern = emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW>;
-	if (!attr_set) {
-		XMG_CK(cudaFuncSetAttribute(kern,
-		    cudaFuncAttributeMaxDynamicSharedMemorySize, SC::SMEM));
-		attr_set = true;
+	if (ws == e->ws)
+		return XMG_OK;
+	for (int side = 0; side < 2; side++) {
+		std::vector<xmgd_view_t> V = side ? e->VB : e->VA;
+		std::vector<char> &use = side ? e->useB : e->useA;
+		for (size_t v = 0; v < V.size(); v++)
+			if (use[v])
+				V[v].slices += ws;
+		XMG_CK(cudaMemcpyAsync((void *)(side ? e->d_vb : e->d_va), V.data(),
+		    V.size() * sizeof(xmgd_view_t), cudaMemcpyHostToDevice, stream()));
+		XMG_CK(cudaStreamSynchronize(stream()));
 	}
-	kern<<<(unsigned)items.size(), 64 + 32 * EMU_DW, SC::SMEM, stream()>>>(
-	    (const emu_item *)d_items, d_cbs, d_prs, (const xmgd_view_t *)d_va,
-	    (const xmgd_view_t *)d_vb, d_tabs, EA, EB, (const int32_t *)d_F,
-	    p->alpha[0], p->beta[0], 2 * fin<TIN>::EXPOFF, cplx, (int *)d_err + 1);
-	g_launches++;
-	XMG_CK(cudaGetLastError());
-	XMG_CK(cudaEventRecord(e2, stream()));
-	XMG_CK(cudaEventSynchronize(e2));
-	float ms1 = 0, ms2 = 0;
-	cudaEventElapsedTime(&ms1, e0, e1);
-	cudaEventElapsedTime(&ms2, e1, e2);
-	tm->ms_split += ms1;
-	tm->ms_gemm += ms2;
-	tm->gemm_launches += 1;
-	tm->gemm_items += (int32_t)items.size();
-	cudaEventDestroy(e0);
-	cudaEventDestroy(e1);
-	cudaEventDestroy(e2);
-	XMG_CK(cudaMemcpy(flags, (void *)d_err, sizeof flags, cudaMemcpyDeviceToHost));
-	if (flags[1])
-		return xmg_seterr(XMG_ETIMEOUT, "split-precision GEMM: bounded "
-		    "wait %d timed out", flags[1]);
+	e->ws = ws;
+	*moved = true;
 	return XMG_OK;
 }
 
-int
-emu_contract(xmgd_contract_t *p, const std::vector<int> &cblocks,
-    const xmgd_cblock_t *d_cbs, const xmgd_pair_t *d_prs,
-    const int32_t *d_tabs, xmgd_timing_t *tm)
-{
-	const bool realab = p->alpha[1] == 0 && p->beta[1] == 0;
+int emu_current(const emu_plan *e) { return e->cur; }
+int emu_ncand(const emu_plan *e) { return (int)e->cand.size(); }
+bool emu_tuned(const emu_plan *e) { return e->tuned != 0; }
 
-	switch (p->dtype) {
-	case 0:
-		return run_emu<float, float>(p, cblocks, d_cbs, d_prs, d_tabs, tm, 0);
-	case 2:
-		return run_emu<double, double>(p, cblocks, d_cbs, d_prs, d_tabs, tm, 0);
-	case 1:
-	case 3:
-		/* two real passes need real alpha and beta */
-		if (!realab)
-			return xmg_seterr(XMG_ENOTSUP, "split-precision path: complex "
-			    "alpha/beta");
-		return p->dtype == 1 ?
-		    run_emu<float, float>(p, cblocks, d_cbs, d_prs, d_tabs, tm, 1) :
-		    run_emu<double, double>(p, cblocks, d_cbs, d_prs, d_tabs, tm, 1);
+int emu_record_split(emu_plan *e) { return e->split(e); }
+int emu_record_gemm(emu_plan *e) { return e->gemm(e); }
+int64_t emu_slice_bytes(const emu_plan *e) { return (int64_t)e->slice_bytes; }
+int emu_items(const emu_plan *e) { return e->cand[e->cur].nitems; }
+
+/* after the stream has drained: flags, then one tuning step with the
+ * measured GEMM time of the candidate that ran */
+int
+emu_finish(emu_plan *e, float gemm_ms, int *nan)
+{
+	*nan = e->h_flags[0] & 1;
+	if (e->h_flags[1])
+		return xmg_seterr(XMG_ETIMEOUT, "split-precision GEMM: bounded "
+		    "wait %d timed out", e->h_flags[1]);
+	if (!e->tuned && !*nan) {
+		e->cand[e->cur].ms = gemm_ms;
+		if (e->cur + 1 < (int)e->cand.size())
+			e->cur++;
+		else {
+			int best = 0;
+			for (int i = 1; i < (int)e->cand.size(); i++)
+				if (e->cand[i].ms < e->cand[best].ms)
+					best = i;
+			e->cur = best;
+			e->tuned = 1;
+			g_tuned.push_back(tune_entry{e->sig, e->cand[best].policy});
+		}
 	}
-	return xmg_seterr(XMG_ENOTSUP, "split-precision path: scalar type");
+	return XMG_OK;
 }
 
 } /* namespace xmg */

@@ -19,6 +19,7 @@
  */
 #include <stdlib.h>
 #include <string.h>
+#include <vector>
 
 #include "common.cuh"
 
@@ -203,24 +204,12 @@ launch(const xmgd_ptask_t *dtasks, const task_meta *dmeta, int ntasks,
 	return check(cudaGetLastError(), "ptask_kernel launch");
 }
 
-} /* namespace xmg */
-
-using namespace xmg;
-
-extern "C" int
-xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
-    double *dots)
+/* CTA schedule of every task of a batch; returns the grid size */
+static int64_t
+plan_tasks(const xmgd_ptask_t *tasks, int ntasks, task_meta *meta)
 {
-	task_meta *meta;
 	int64_t nctas = 0;
-	uint64_t dbuf, dpart = 0;
-	size_t tb, mb, k;
-	int st, has_dot = dots != nullptr;
 
-	if (ntasks <= 0)
-		return XMG_OK;
-	if ((meta = (task_meta *)calloc((size_t)ntasks, sizeof *meta)) == NULL)
-		return xmg_seterr(XMG_ENOMEM, "out of memory");
 	for (int i = 0; i < ntasks; i++) {
 		const xmgd_ptask_t &t = tasks[i];
 		task_meta &m = meta[i];
@@ -251,6 +240,90 @@ xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
 			    ((m.nouter + rows - 1) / rows);
 		}
 	}
+	return nctas;
+}
+
+static int
+launch_types(int dtype, int stype, const xmgd_ptask_t *dt, const task_meta *dm,
+    int ntasks, int64_t nctas, double *dp)
+{
+	int st;
+
+#define L(D, S) st = launch<D, S>(dt, dm, ntasks, nctas, dp)
+	if (dtype == stype) {
+		switch (dtype) {
+		case 0: L(float, float); break;
+		case 1: L(cf, cf); break;
+		case 2: L(double, double); break;
+		case 3: L(cd, cd); break;
+		default: st = xmg_seterr(XMG_EINVAL, "bad scalar type");
+		}
+	} else if (dtype == 2 && stype == 0) L(double, float);
+	else if (dtype == 0 && stype == 2) L(float, double);
+	else if (dtype == 3 && stype == 1) L(cd, cf);
+	else if (dtype == 1 && stype == 3) L(cf, cd);
+	else st = xmg_seterr(XMG_EINVAL, "unsupported scalar conversion");
+#undef L
+	return st;
+}
+
+static size_t
+task_bytes(int ntasks)
+{
+	return ((size_t)ntasks * sizeof(xmgd_ptask_t) + 255) & ~(size_t)255;
+}
+
+} /* namespace xmg */
+
+using namespace xmg;
+
+extern "C" int
+xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, uint64_t *dbuf,
+    int64_t *nctas)
+{
+	std::vector<task_meta> meta((size_t)ntasks);
+	const size_t tb = task_bytes(ntasks);
+	int st;
+
+	*dbuf = 0;
+	*nctas = plan_tasks(tasks, ntasks, meta.data());
+	if ((st = xmgd_alloc(tb + meta.size() * sizeof(task_meta), dbuf)))
+		return st;
+	XMG_CK(cudaMemcpyAsync((void *)*dbuf, tasks, (size_t)ntasks *
+	    sizeof(xmgd_ptask_t), cudaMemcpyHostToDevice, stream()));
+	XMG_CK(cudaMemcpyAsync((void *)(*dbuf + tb), meta.data(), meta.size() *
+	    sizeof(task_meta), cudaMemcpyHostToDevice, stream()));
+	/* the host copies are the caller's: finish before returning */
+	XMG_CK(cudaStreamSynchronize(stream()));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_ptask_launch(int dtype, int stype, uint64_t dbuf, int ntasks,
+    int64_t nctas)
+{
+	if (ntasks <= 0)
+		return XMG_OK;
+	return launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
+	    (const task_meta *)(dbuf + task_bytes(ntasks)), ntasks, nctas,
+	    nullptr);
+}
+
+extern "C" int
+xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
+    double *dots)
+{
+	task_meta *meta;
+	int64_t nctas = 0;
+	uint64_t dbuf, dpart = 0;
+	size_t tb, mb, k;
+	int st, has_dot = dots != nullptr;
+
+	if (ntasks <= 0)
+		return XMG_OK;
+	if ((meta = (task_meta *)calloc((size_t)ntasks, sizeof *meta)) == NULL)
+		return xmg_seterr(XMG_ENOMEM, "out of memory");
+	nctas = plan_tasks(tasks, ntasks, meta);
 	tb = (size_t)ntasks * sizeof(xmgd_ptask_t);
 	mb = (size_t)ntasks * sizeof(task_meta);
 	tb = (tb + 255) & ~(size_t)255;
@@ -266,26 +339,8 @@ xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
 	if (has_dot && (st = xmgd_scratch(3, (size_t)nctas * 2 *
 	    sizeof(double), &dpart)) != XMG_OK)
 		goto out;
-	{
-		const xmgd_ptask_t *dt = (const xmgd_ptask_t *)dbuf;
-		const task_meta *dm = (const task_meta *)(dbuf + tb);
-		double *dp = (double *)dpart;
-#define L(D, S) st = launch<D, S>(dt, dm, ntasks, nctas, dp)
-		if (dtype == stype) {
-			switch (dtype) {
-			case 0: L(float, float); break;
-			case 1: L(cf, cf); break;
-			case 2: L(double, double); break;
-			case 3: L(cd, cd); break;
-			default: st = xmg_seterr(XMG_EINVAL, "bad scalar type");
-			}
-		} else if (dtype == 2 && stype == 0) L(double, float);
-		else if (dtype == 0 && stype == 2) L(float, double);
-		else if (dtype == 3 && stype == 1) L(cd, cf);
-		else if (dtype == 1 && stype == 3) L(cf, cd);
-		else st = xmg_seterr(XMG_EINVAL, "unsupported scalar conversion");
-#undef L
-	}
+	st = launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
+	    (const task_meta *)(dbuf + tb), ntasks, nctas, (double *)dpart);
 	if (st != XMG_OK)
 		goto out;
 	/* the task buffers are reused by the next batch: wait here */

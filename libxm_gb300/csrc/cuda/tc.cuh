@@ -68,15 +68,20 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
 	if (mbar_try(bar, parity))
 		return true;
 	uint64_t t0 = gtimer();
-	for (;;) {
+	for (uint32_t n = 1;; n++) {
 		if (mbar_try(bar, parity))
 			return true;
-		if (*s_err)
-			return false;
-		if (gtimer() - t0 > WAIT_NS) {
-			*s_err = code;
-			atomicMax(g_err, code);
-			return false;
+		/* the failure flag and the clock only every 16th poll: each
+		 * shared-memory read competes with the tensor core's operand
+		 * reads */
+		if ((n & 15) == 0) {
+			if (*s_err)
+				return false;
+			if (gtimer() - t0 > WAIT_NS) {
+				*s_err = code;
+				atomicMax(g_err, code);
+				return false;
+			}
 		}
 	}
 }

@@ -295,6 +295,53 @@ cand_hash(const xm_tensor_t *a, const xm_tensor_t *b, const struct cand *x,
 	return h == XMG_HMAP_EMPTY ? h - 1 : h;
 }
 
+/*
+ * Order of the contracted indices inside one pair's K.  Any order gives the
+ * same sum as long as both operands of the pair use it, so K follows the
+ * memory order of the larger operand block that holds a unit-stride
+ * contracted index: its K rows are then contiguous runs, and the unfold
+ * gathers of the split kernels read whole sectors.  Without such an index
+ * the masks' own order stays.
+ */
+static void
+k_order(const xm_dim_t *cidxa, const xm_dim_t *cidxb, const int64_t *sa,
+    const int64_t *sb, int64_t na, int64_t nb, xm_dim_t *ka, xm_dim_t *kb)
+{
+	const int64_t *st = NULL;
+	const xm_dim_t *mk = NULL;
+	size_t q, r, n = cidxa->n;
+	int hasa = 0, hasb = 0;
+
+	*ka = *cidxa;
+	*kb = *cidxb;
+	for (q = 0; q < n; q++) {
+		hasa |= sa[cidxa->i[q]] == 1;
+		hasb |= sb[cidxb->i[q]] == 1;
+	}
+	if (hasb && (!hasa || nb >= na)) {
+		st = sb;
+		mk = cidxb;
+	} else if (hasa) {
+		st = sa;
+		mk = cidxa;
+	} else
+		return;
+	/* insertion sort of the positions by the chosen side's strides */
+	for (q = 1; q < n; q++) {
+		size_t ia = ka->i[q], ib = kb->i[q];
+		int64_t key = st[mk == cidxb ? ib : ia];
+		for (r = q; r > 0; r--) {
+			int64_t prev = st[mk == cidxb ? kb->i[r - 1] : ka->i[r - 1]];
+			if (prev <= key)
+				break;
+			ka->i[r] = ka->i[r - 1];
+			kb->i[r] = kb->i[r - 1];
+		}
+		ka->i[r] = ia;
+		kb->i[r] = ib;
+	}
+}
+
 static double
 now_ms(void)
 {
@@ -359,7 +406,7 @@ static int
 build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, plan_t *p, int device)
 {
-	xm_dim_t *list, nba, nbb, blkc, ia, ib, dims, dA, dB;
+	xm_dim_t *list, nba, nbb, blkc, ia, ib, dims, dA, dB, ka, kb;
 	size_t nlist, nblkk, l, i;
 	struct cand *cand = NULL;
 	xmg_hmap_t merge;
@@ -467,9 +514,11 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 				continue;
 			xmg_tensor_block_strides(a, cand[i].ia, sa);
 			xmg_tensor_block_strides(b, cand[i].ib, sb);
-			arow = mask_table(&p->tabs, &dA, sa, &p->cidxa);
+			k_order(&p->cidxa, &p->cidxb, sa, sb,
+			    (int64_t)pr->k * cb->m, (int64_t)pr->k * cb->n, &ka, &kb);
+			arow = mask_table(&p->tabs, &dA, sa, &ka);
 			acol = mask_table(&p->tabs, &dA, sa, &p->aidxa);
-			brow = mask_table(&p->tabs, &dB, sb, &p->cidxb);
+			brow = mask_table(&p->tabs, &dB, sb, &kb);
 			bcol = mask_table(&p->tabs, &dB, sb, &p->aidxb);
 			pr->arow = arow; pr->acol = acol;
 			pr->brow = brow; pr->bcol = bcol;
@@ -552,27 +601,139 @@ xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
 	return st;
 }
 
+/* ------------------------------------------------------------------ */
+/* plan cache                                                          */
+
+/*
+ * Contractions repeat: an iterative solver calls the same xm_contract
+ * every iteration on tensors whose block structure never changes.  A
+ * device plan (uploaded metadata, work lists, captured CUDA graph) is kept
+ * per (a, b, c, their structure generations, index strings, alpha, beta,
+ * precision) and replayed; any block-table change draws a new generation,
+ * so a stale plan can never match.  Only tensors whose blocks live in GPU
+ * memory are cached (pagefile blocks are staged per call).
+ */
+#define PC_MAX 16
+
+struct pc_entry {
+	const xm_tensor_t *a, *b, *c;
+	uint64_t ga, gb, gc;
+	char idx[3][16];
+	xm_scalar_t alpha, beta;
+	int precision;
+	xmgd_plan_t *dp;
+	double flops;
+	int ncb, npr;
+	uint64_t used;
+};
+static struct pc_entry g_pc[PC_MAX];
+static uint64_t g_pc_tick;
+static int g_pc_slots = -1;
+
+static int
+pc_slots(void)
+{
+	const char *e;
+
+	if (g_pc_slots < 0) {
+		g_pc_slots = 8;
+		if ((e = getenv("XMG_PLAN_CACHE")) != NULL)
+			g_pc_slots = atoi(e);
+		if (g_pc_slots < 0)
+			g_pc_slots = 0;
+		if (g_pc_slots > PC_MAX)
+			g_pc_slots = PC_MAX;
+	}
+	return g_pc_slots;
+}
+
+static int
+pc_match(const struct pc_entry *e, xm_scalar_t alpha, const xm_tensor_t *a,
+    const xm_tensor_t *b, xm_scalar_t beta, const xm_tensor_t *c,
+    const char *idxa, const char *idxb, const char *idxc, int prec)
+{
+	return e->dp != NULL && e->a == a && e->b == b && e->c == c &&
+	    e->ga == a->gen && e->gb == b->gen && e->gc == c->gen &&
+	    e->alpha == alpha && e->beta == beta && e->precision == prec &&
+	    strcmp(e->idx[0], idxa) == 0 && strcmp(e->idx[1], idxb) == 0 &&
+	    strcmp(e->idx[2], idxc) == 0;
+}
+
+static void
+pc_drop(struct pc_entry *e)
+{
+	if (e->dp)
+		xmgd_plan_free(e->dp);
+	memset(e, 0, sizeof *e);
+}
+
+void
+xmg_plan_cache_clear(void)
+{
+	int i;
+
+	for (i = 0; i < PC_MAX; i++)
+		pc_drop(&g_pc[i]);
+}
+
+static void
+stats_from(double flops, int ncb, int npr, int precision_used, double t0)
+{
+	xmgd_timing_t tm;
+
+	xmgd_last_timing(&tm);
+	g_stats.flops = flops;
+	g_stats.ms_device = tm.ms_total;
+	g_stats.ms_split = tm.ms_split;
+	g_stats.ms_gemm = tm.ms_gemm;
+	g_stats.n_cblocks = ncb;
+	g_stats.n_pairs = npr;
+	g_stats.slice_bytes = tm.slice_bytes;
+	g_stats.precision_used = precision_used;
+	g_stats.gemm_launches = tm.gemm_launches;
+	(void)t0;
+}
+
 int
 xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
     xm_scalar_t beta, xm_tensor_t *c, const char *idxa, const char *idxb,
     const char *idxc)
 {
 	xmgd_contract_t dp;
-	xmgd_timing_t tm;
+	xmgd_plan_t *h = NULL;
+	struct pc_entry *e = NULL;
 	plan_t p;
 	double t0 = now_ms();
-	int st, l;
+	int st, l, i, prec = precision_mode(), used = XMG_PREC_FP64, cache;
 
 	init_plan(&p);
 	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) != XMG_OK)
 		goto out;
 	if ((st = xmgd_init()) != XMG_OK)
 		goto out;
+	memset(&g_stats, 0, sizeof g_stats);
+	cache = pc_slots() > 0 && xmg_alloc_is_device(c->allocator) &&
+	    strlen(idxa) < 16 && strlen(idxb) < 16 && strlen(idxc) < 16;
+	if (cache) {
+		for (i = 0; i < pc_slots(); i++)
+			if (pc_match(&g_pc[i], alpha, a, b, beta, c, idxa, idxb,
+			    idxc, prec))
+				e = &g_pc[i];
+		if (e) {
+			e->used = ++g_pc_tick;
+			g_stats.ms_plan = now_ms() - t0;
+			st = xmgd_plan_run(e->dp, &used);
+			stats_from(e->flops, e->ncb, e->npr, used, t0);
+			if (st != XMG_OK)
+				pc_drop(e);
+			goto out;
+		}
+	}
 	if ((st = build_plan(alpha, a, b, c, &p, 1)) != XMG_OK)
 		goto out;
 	memset(&dp, 0, sizeof dp);
 	dp.dtype = c->type;
-	dp.precision = precision_mode();
+	dp.precision = prec;
 	xmg_scalar_pack(alpha, dp.alpha);
 	xmg_scalar_pack(beta, dp.beta);
 	dp.ncblocks = p.ncb;
@@ -589,9 +750,35 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	dp.nexp_b = p.nexp_b;
 	dp.flops = p.flops;
 	dp.emulatable = p.emulatable;
-	memset(&g_stats, 0, sizeof g_stats);
+	if ((st = xmgd_plan_create(&dp, &h)) != XMG_OK)
+		goto out;
 	g_stats.ms_plan = now_ms() - t0;
-	st = xmgd_contract(&dp);
+	st = xmgd_plan_run(h, &used);
+	stats_from(p.flops, p.ncb, p.npr, used, t0);
+	if (cache && st == XMG_OK) {
+		/* keep it: the least recently used slot gives way */
+		e = &g_pc[0];
+		for (i = 1; i < pc_slots(); i++)
+			if (g_pc[i].used < e->used)
+				e = &g_pc[i];
+		pc_drop(e);
+		e->a = a; e->b = b; e->c = c;
+		e->ga = a->gen; e->gb = b->gen; e->gc = c->gen;
+		strcpy(e->idx[0], idxa);
+		strcpy(e->idx[1], idxb);
+		strcpy(e->idx[2], idxc);
+		e->alpha = alpha;
+		e->beta = beta;
+		e->precision = prec;
+		e->dp = h;
+		e->flops = p.flops;
+		e->ncb = p.ncb;
+		e->npr = p.npr;
+		e->used = ++g_pc_tick;
+		h = NULL;
+	}
+	if (h)
+		xmgd_plan_free(h);
 	if (st == XMG_OK && !xmg_alloc_is_device(c->allocator)) {
 		for (l = 0; l < p.ncb && st == XMG_OK; l++) {
 			xm_dim_t *list; size_t n;
@@ -605,16 +792,6 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		}
 		xmg_alloc_release_views(c->allocator, 0);
 	}
-	xmgd_last_timing(&tm);
-	g_stats.flops = p.flops;
-	g_stats.ms_device = tm.ms_total;
-	g_stats.ms_split = tm.ms_split;
-	g_stats.ms_gemm = tm.ms_gemm;
-	g_stats.n_cblocks = p.ncb;
-	g_stats.n_pairs = p.npr;
-	g_stats.slice_bytes = tm.slice_bytes;
-	g_stats.precision_used = dp.precision_used;
-	g_stats.gemm_launches = tm.gemm_launches;
 out:
 	plan_free(&p);
 	return st;

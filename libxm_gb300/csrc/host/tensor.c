@@ -59,6 +59,17 @@ xmg_tensor_block_strides(const xm_tensor_t *t, xm_dim_t blkidx,
 		strides[k] = cs[b->perm.i[k]];
 }
 
+/* Every block-table change draws a fresh generation number, so a cached
+ * contraction plan keyed on (tensor address, generation) can never match a
+ * tensor that changed or a new tensor at a recycled address. */
+static uint64_t g_gen;
+
+void
+xmg_tensor_touch(xm_tensor_t *t)
+{
+	t->gen = __atomic_add_fetch(&g_gen, 1, __ATOMIC_RELAXED);
+}
+
 xm_tensor_t *
 xm_tensor_create(const xm_block_space_t *bs, xm_scalar_type_t type,
     xm_allocator_t *allocator)
@@ -86,6 +97,7 @@ xm_tensor_create(const xm_block_space_t *bs, xm_scalar_type_t type,
 		t->blocks[i].scalar = 0;
 		t->blocks[i].data = XM_NULL_PTR;
 	}
+	xmg_tensor_touch(t);
 	return t;
 }
 
@@ -120,6 +132,7 @@ xm_tensor_create_structure(const xm_tensor_t *src, xm_scalar_type_t type,
 			xm_tensor_set_canonical_block(t, idx);
 		}
 	}
+	xmg_tensor_touch(t);
 	return t;
 }
 
@@ -222,6 +235,7 @@ xm_tensor_set_zero_block(xm_tensor_t *t, xm_dim_t blkidx)
 	b->perm = xm_dim_identity_permutation(blkidx.n);
 	b->scalar = 0;
 	b->data = XM_NULL_PTR;
+	xmg_tensor_touch(t);
 }
 
 void
@@ -253,6 +267,7 @@ xm_tensor_set_canonical_block_raw(xm_tensor_t *t, xm_dim_t blkidx,
 	b->perm = xm_dim_identity_permutation(blkidx.n);
 	b->scalar = 1;
 	b->data = data_ptr;
+	xmg_tensor_touch(t);
 }
 
 void
@@ -278,6 +293,7 @@ xm_tensor_set_derivative_block(xm_tensor_t *t, xm_dim_t blkidx,
 	b->perm = permutation;
 	b->scalar = scalar;
 	b->data = xmg_tensor_block_linear(t, source_blkidx);
+	xmg_tensor_touch(t);
 }
 
 void
@@ -444,6 +460,7 @@ xm_tensor_free_block_data(xm_tensor_t *t)
 		t->blocks[i].scalar = 0;
 		t->blocks[i].data = XM_NULL_PTR;
 	}
+	xmg_tensor_touch(t);
 }
 
 void

@@ -53,6 +53,13 @@ typedef struct {
 
 /* dtype/stype: xm_scalar_type_t values.  For XMGD_OP_DOT the per-task dot
  * products (complex: re, im) are written to dots[2*ntasks] (host). */
+/* A batch uploaded once into a device buffer owned by the caller (release
+ * with xmgd_free) and launched any number of times, also under stream
+ * capture. */
+int xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, uint64_t *dbuf,
+    int64_t *nctas);
+int xmgd_ptask_launch(int dtype, int stype, uint64_t dbuf, int ntasks,
+    int64_t nctas);
 int xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
     double *dots);
 
@@ -112,6 +119,15 @@ typedef struct {
 } xmgd_contract_t;
 
 int xmgd_contract(xmgd_contract_t *plan);
+
+/* Reusable device plan of one contraction: the uploaded metadata, operand
+ * views and work lists, and the whole launch sequence captured once as a
+ * CUDA graph.  Built from a host plan (whose arrays may be freed right
+ * after), replayed by xmgd_plan_run. */
+typedef struct xmgd_plan xmgd_plan_t;
+int xmgd_plan_create(const xmgd_contract_t *p, xmgd_plan_t **out);
+int xmgd_plan_run(xmgd_plan_t *dp, int *precision_used);
+void xmgd_plan_free(xmgd_plan_t *dp);
 
 /* Timing of the last xmgd_contract, milliseconds (device events). */
 typedef struct {

@@ -38,7 +38,11 @@ struct xm_tensor {
 	xm_allocator_t *allocator;
 	struct xmg_block *blocks;
 	size_t nblocks_total;
+	uint64_t gen;            /* structure generation, unique per change */
 };
+
+/* new structure generation for t (block table changed) */
+void xmg_tensor_touch(xm_tensor_t *t);
 
 /* allocator internals used by the contraction engine */
 int xmg_alloc_is_device(const xm_allocator_t *a);
