@@ -292,6 +292,39 @@ __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 	return min(lim, c0 + EMU_CHUNK);
 }
 
+/* Accumulators: 0, 1, 2 hold the exact weight groups p + q = 0, 1, 2; 3
+ * the low band p + q = 3..KEEP.  The top one (3 with a low band, else 2)
+ * forms set X, the others set Y.  The drain reads X first and releases it,
+ * so at a chunk boundary the MMA warp issues the X products of the next
+ * chunk's first (already staged) K steps while the drain still reads Y. */
+template <int KEEP>
+struct acc_sets {
+	static constexpr int XACC = KEEP > 2 ? 3 : 2;
+};
+
+/* the slice products of one K step whose accumulator lies in `which`
+ * (1: set X, 2: set Y, 3: both) */
+template <int S, int KEEP>
+__device__ __forceinline__ void
+issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
+    int which, uint32_t &started)
+{
+#pragma unroll
+	for (int pa = 0; pa < S; pa++)
+#pragma unroll
+		for (int qb = 0; qb < S; qb++) {
+			if (pa + qb > KEEP)
+				continue;
+			const int acc = min(pa + qb, 3);
+			if (!(which & (acc == acc_sets<KEEP>::XACC ? 1 : 2)))
+				continue;
+			uint64_t ad = sdesc(base + qb * 256, S * 256);
+			uint64_t bd = sdesc(base + a_off + pa * 256, S * 256);
+			mma_bf16(tmem + acc * 128, ad, bd, idesc, (started >> acc) & 1u);
+			started |= 1u << acc;
+		}
+}
+
 template <int S, int KEEP, bool LOW, typename TOUT, int DW>
 __global__ void __launch_bounds__(64 + 32 * DW, 1)
 emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
@@ -307,7 +340,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 	uint8_t *stages = reinterpret_cast<uint8_t *>(
 	    (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
 	__shared__ __align__(8) uint64_t bar_full[NST], bar_empty[NST];
-	__shared__ __align__(8) uint64_t bar_accfull, bar_accempty, bar_fin;
+	__shared__ __align__(8) uint64_t bar_accfull, bar_xempty, bar_yempty, bar_fin;
 	__shared__ __align__(8) uint64_t bar_ifull[2], bar_iempty[2];
 	__shared__ int s_item[2];
 	__shared__ uint32_t s_tmem;
@@ -326,7 +359,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			mbar_init(smem_u32(&bar_empty[s]), 1);
 		}
 		mbar_init(smem_u32(&bar_accfull), 1);
-		mbar_init(smem_u32(&bar_accempty), DW);
+		mbar_init(smem_u32(&bar_xempty), DW);
+		mbar_init(smem_u32(&bar_yempty), DW);
 		mbar_init(smem_u32(&bar_fin), 1);
 		for (int q = 0; q < 2; q++) {
 			mbar_init(smem_u32(&bar_ifull[q]), 1);
@@ -421,7 +455,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 		if (lane == 0) {
 			int s = 0;
 			bool first = true;
-			uint32_t ph = 0, eph = 0;
+			uint32_t ph = 0, xph = 0, yph = 0;
 			uint32_t iph = 0;
 			for (int slot = 0; !s_err; ) {
 				if (!mbar_wait(smem_u32(&bar_ifull[slot]), iph, &s_err, g_err, 6))
@@ -439,40 +473,58 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					const int nks = vb[pr.bview].n_ks;
 					for (int c0 = 0; c0 < nks && !s_err; ) {
 						const int c1 = chunk_end(c0, nks, cplx);
-						/* the accumulators are free once the drain warps
-						 * have read the previous chunk (of this or the
-						 * previous item) */
-						if (!first) {
-							if (!mbar_wait(smem_u32(&bar_accempty), eph, &s_err, g_err, 2))
-								break;
-							eph ^= 1;
-						}
-						first = false;
-						tc_fence_after();
+						const int L = min(NST, c1 - c0);
 						/* every accumulator restarts each chunk: the exact
 						 * groups for their 2^23 bound, the low band because
 						 * the tensor core's fp32 accumulation error grows
 						 * with the accumulation length (per-pair
 						 * accumulation measured 10x larger error) */
 						uint32_t started = 0;
-						for (int ks = c0; ks < c1; ks++) {
+						bool okc = true;
+						/* set X of the first L (staged) K steps, as soon as
+						 * the drain has read X of the previous chunk */
+						if (!first) {
+							if (!mbar_wait(smem_u32(&bar_xempty), xph, &s_err, g_err, 2))
+								break;
+							xph ^= 1;
+						}
+						tc_fence_after();
+						for (int j = 0; j < L; j++) {
+							const int sj = s + j < NST ? s + j : s + j - NST;
+							const uint32_t pj = s + j < NST ? ph : ph ^ 1;
+							if (!mbar_wait(smem_u32(&bar_full[sj]), pj, &s_err, g_err, 3)) {
+								okc = false;
+								break;
+							}
+							tc_fence_after();
+							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
+						}
+						if (!okc)
+							break;
+						/* set Y of the same steps once Y is read too */
+						if (!first) {
+							if (!mbar_wait(smem_u32(&bar_yempty), yph, &s_err, g_err, 8))
+								break;
+							yph ^= 1;
+						}
+						first = false;
+						tc_fence_after();
+						for (int j = 0; j < L; j++) {
+							const int sj = s + j < NST ? s + j : s + j - NST;
+							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
+							mma_commit(smem_u32(&bar_empty[sj]));
+						}
+						s += L;
+						if (s >= NST) { s -= NST; ph ^= 1; }
+						/* the rest of the chunk: every product per step */
+						for (int ks = c0 + L; ks < c1; ks++) {
 							if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3))
 								break;
 							tc_fence_after();
-							const uint32_t base = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
-#pragma unroll
-							for (int pa = 0; pa < S; pa++)
-#pragma unroll
-								for (int qb = 0; qb < S; qb++) {
-									if (pa + qb > KEEP)
-										continue;
-									const int acc = min(pa + qb, 3);
-									uint64_t ad = sdesc(base + qb * 256, S * 256);
-									uint64_t bd = sdesc(base + C::CHUNK_BYTES + pa * 256, S * 256);
-									mma_bf16(tmem + acc * 128, ad, bd, idesc,
-									    (started >> acc) & 1u);
-									started |= 1u << acc;
-								}
+							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)s *
+							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 3, started);
 							mma_commit(smem_u32(&bar_empty[s]));
 							if (++s == NST) { s = 0; ph ^= 1; }
 						}
@@ -544,16 +596,47 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					}
 					fph ^= 1;
 					tc_fence_after();
+					/* set X first: the low band (or, without one, group 2),
+					 * then release it to the MMA warp */
+					constexpr int XACC = acc_sets<KEEP>::XACC;
 #pragma unroll
 					for (int b4 = 0; b4 < NC / 4; b4++) {
 						if (half * NC + b4 * 4 >= rows)
 							break;	/* warp-uniform: columns past the tile */
-						float a0[4], a1[4], a2[4], a3[4];
+						float ax[4];
+						tmem_ld4(trow + XACC * 128 + b4 * 4, ax);
+						tmem_wait_ld();
+#pragma unroll
+						for (int c = 0; c < 4; c++) {
+							if (LOW) {
+								/* low band in units of 2^(-16-F) without a
+								 * 64-bit conversion: x = h * 2^24 + l with
+								 * h = rint(x / 2^24) and l = x - h * 2^24,
+								 * both exact in fp32 and converted as int32 */
+								const float x = ax[c] * s3;
+								const float h = rintf(x * 5.9604644775390625e-8f);
+								const float l = fmaf(h, -16777216.0f, x);
+								V[b4 * 4 + c] += ((long long)__float2int_rn(h) << 24) +
+								    __float2int_rn(l);
+							} else {
+								V[b4 * 4 + c] += (long long)__float2int_rn(ax[c] * s2) << F;
+							}
+						}
+					}
+					tc_fence_before();
+					__syncwarp();
+					if (lane == 0)
+						mbar_arrive(smem_u32(&bar_xempty));
+					/* set Y: the exact groups below X */
+#pragma unroll
+					for (int b4 = 0; b4 < NC / 4; b4++) {
+						if (half * NC + b4 * 4 >= rows)
+							break;
+						float a0[4], a1[4], a2[4];
 						tmem_ld4(trow + 0 * 128 + b4 * 4, a0);
 						tmem_ld4(trow + 1 * 128 + b4 * 4, a1);
-						tmem_ld4(trow + 2 * 128 + b4 * 4, a2);
 						if (LOW)
-							tmem_ld4(trow + 3 * 128 + b4 * 4, a3);
+							tmem_ld4(trow + 2 * 128 + b4 * 4, a2);
 						tmem_wait_ld();
 #pragma unroll
 						for (int c = 0; c < 4; c++) {
@@ -561,27 +644,16 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 							 * |i0 * 256 + i1| < 2^31 */
 							int i0 = __float2int_rn(a0[c] * s0);
 							int i1 = __float2int_rn(a1[c] * s1);
-							int i2 = __float2int_rn(a2[c] * s2);
-							long long d = ((long long)(i0 * 256 + i1) << 8) + i2;
-							long long v = d << F;
-							if (LOW) {
-								/* low band in units of 2^(-16-F) without a
-								 * 64-bit conversion: x = h * 2^24 + l with
-								 * h = rint(x / 2^24) and l = x - h * 2^24,
-								 * both exact in fp32 and converted as int32 */
-								const float x = a3[c] * s3;
-								const float h = rintf(x * 5.9604644775390625e-8f);
-								const float l = fmaf(h, -16777216.0f, x);
-								v += ((long long)__float2int_rn(h) << 24) +
-								    __float2int_rn(l);
-							}
-							V[b4 * 4 + c] += v;
+							long long d = (long long)(i0 * 256 + i1) << 8;
+							if (LOW)
+								d += __float2int_rn(a2[c] * s2);
+							V[b4 * 4 + c] += d << F;
 						}
 					}
 					tc_fence_before();
 					__syncwarp();
 					if (lane == 0)
-						mbar_arrive(smem_u32(&bar_accempty));
+						mbar_arrive(smem_u32(&bar_yempty));
 					c0 = c1;
 				}
 			}
