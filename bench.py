@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
+    p.add_argument("--subset", type=str, default=None,
+                   help="O,V: keep the first O occupied and V virtual blocks (profiling case)")
     return p.parse_args()
 
 
@@ -150,7 +152,7 @@ def cpu_baseline(w, ranks, target_s, engine_out=None):
     from libxm_gb300 import api, workloads as W
     lib, kind = cpu_lib()
     al = api.Allocator(lib)
-    wc = make_workload(lib, al, w.scale)
+    wc = make_workload(lib, al, w.scale, w.subset)
     blocks = wc.c.canonical_blocks()
     cost = block_costs(wc)
 
@@ -207,7 +209,7 @@ def block_costs(w):
     orig = W.fill
     W.fill = lambda *x, **y: None
     try:
-        wo = make_workload(orc, oal, w.scale)
+        wo = make_workload(orc, oal, w.scale, w.subset)
     finally:
         W.fill = orig
     import helpers as H
@@ -219,10 +221,12 @@ def block_costs(w):
     return cost
 
 
-def make_workload(lib, al, scale=1):
+def make_workload(lib, al, scale=1, subset=None):
     from libxm_gb300 import workloads as W
-    w = W.cfg2(lib, al, scale=scale)
+    ob, vb = (int(x) for x in subset.split(",")) if subset else (None, None)
+    w = W.cfg2(lib, al, scale=scale, o_blocks=ob, v_blocks=vb)
     w.scale = scale
+    w.subset = subset
     return w
 
 
@@ -235,7 +239,7 @@ def engine_arm(args, ranks):
     eng = libxm_gb300.load()
     al = api.Allocator(eng)
     t0 = time.perf_counter()
-    w = make_workload(eng, al, args.scale)
+    w = make_workload(eng, al, args.scale, args.subset)
     setup_s = time.perf_counter() - t0
     flops = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
 
@@ -291,23 +295,34 @@ def engine_arm(args, ranks):
             outs[blk] = (p, n)
             nbytes_out += n
         steps = max(1, min(args.steps, 3))
+        writes = [(t.h, api.Dim.of(blk), host[(id(t), blk)][0])
+                  for t in (w.a, w.b) for blk in t.canonical_blocks()]
+        reads = [(w.c.h, api.Dim.of(blk), p) for blk, (p, n) in outs.items()]
+        phase = np.zeros(3)
 
         def e2e_step():
-            for t in (w.a, w.b):
-                for blk in t.canonical_blocks():
-                    eng.xm_tensor_write_block(t.h, api.Dim.of(blk), host[(id(t), blk)][0])
+            t0 = time.perf_counter()
+            for h, d, p in writes:
+                eng.xm_tensor_write_block(h, d, p)
+            t1 = time.perf_counter()
             w.run()
-            for blk, (p, n) in outs.items():
-                eng.xm_tensor_read_block(w.c.h, api.Dim.of(blk), p)
+            t2 = time.perf_counter()
+            for h, d, p in reads:
+                eng.xm_tensor_read_block(h, d, p)
+            phase[:] += (t1 - t0, t2 - t1, time.perf_counter() - t2)
         e2e_step()
         ranks.barrier()
+        phase[:] = 0
         t0 = time.perf_counter()
         for _ in range(steps):
             e2e_step()
         dt = ranks.max((time.perf_counter() - t0) / steps)
         e2e = {"value": ranks.world * flops / dt / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": nbytes_out,
-               "ms_per_step": dt * 1e3}
+               "ms_per_step": dt * 1e3,
+               "phases_ms": {"h2d": phase[0] * 1e3 / steps, "contract": phase[1] * 1e3 / steps,
+                             "d2h": phase[2] * 1e3 / steps},
+               "copies_per_step": len(writes) + len(reads)}
         for p, _ in host.values():
             eng.xmg_host_free(p)
         for p, _ in outs.values():
@@ -368,7 +383,7 @@ def reference_arm(args, ranks):
     from libxm_gb300 import api, workloads as W
     lib, kind = cpu_lib()
     al = api.Allocator(lib)
-    w = make_workload(lib, al, args.scale)
+    w = make_workload(lib, al, args.scale, args.subset)
     cost = block_costs(w)
     blocks = w.c.canonical_blocks()
     total = sum(cost)

@@ -183,16 +183,25 @@ def cfg2_shape(seed=2):
     return o, v, lo, lv
 
 
-def cfg2(lib, alloc, seed=2, scale=1):
+def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None):
     """Uneven-block Z2^3-sparse FP64 ladder: o = 96 in 6 blocks of 8..24,
     v = 384 in 12 blocks of 16..48.  scale > 1 shrinks every block size by
-    that factor (structure preserved) for quick parity runs."""
+    that factor (structure preserved) for quick parity runs; o_blocks /
+    v_blocks keep only the first blocks of each space (block sizes
+    unchanged), a smaller case with the full-size tiles for profiling."""
     o, v, lo, lv = cfg2_shape(seed)
     if scale > 1:
         o = [max(1, x // scale) for x in o]
         v = [max(1, x // scale) for x in v]
+    if o_blocks:
+        o, lo = o[:o_blocks], lo[:o_blocks]
+    if v_blocks:
+        v, lv = v[:v_blocks], lv[:v_blocks]
     w = ladder(lib, alloc, o, v, seed, z2=(lo, lv))
-    w.name = "cfg2_ladder_o96_v384_z2" if scale == 1 else "cfg2_ladder_scaled_%d" % scale
+    if o_blocks or v_blocks:
+        w.name = "cfg2_subset_o%d_v%d" % (len(o), len(v))
+    else:
+        w.name = "cfg2_ladder_o96_v384_z2" if scale == 1 else "cfg2_ladder_scaled_%d" % scale
     w.extra = {"o_sizes": o, "v_sizes": v, "o_labels": lo, "v_labels": lv}
     return w
 
