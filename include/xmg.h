@@ -83,8 +83,23 @@ typedef struct {
 	long long slice_bytes;   /* bytes of staged operand slices */
 	int precision_used;      /* XMG_PREC_FP64 or XMG_PREC_EMU64 */
 	int gemm_launches;       /* kernels launched for the GEMM phase */
+	long long stage_bytes;   /* out-of-core: b bytes streamed into HBM */
+	int stage_batches;       /* out-of-core: batches (0: in-core) */
+	int pad_;
+	double ms_stage_wait;    /* out-of-core: host wait for staging beyond
+	                            the overlapped compute, wall clock */
 } xmg_stats_t;
 int xmg_get_last_stats(xmg_stats_t *out);
+
+/* Out-of-core contractions.  When the pagefile blocks of b that a
+ * contraction reads exceed `budget` bytes, b is streamed through HBM in
+ * batches of at most `region` bytes: two device regions alternate, each
+ * batch is read from the pagefile into pinned chunks and copied on a side
+ * stream while the previous batch is contracted (c accumulates over the
+ * batches; beta is applied once).  a and c are staged whole.  Defaults:
+ * 180 GB and 32 GB, or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps
+ * the current value. */
+int xmg_set_staging(size_t budget, size_t region);
 
 /* Hand-written adjoint of c = alpha * a * b over the index strings.  Given
  * dc (same structure as c), accumulates into the canonical blocks of da

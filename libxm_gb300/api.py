@@ -56,7 +56,9 @@ class Stats(C.Structure):
                 ("ms_device", C.c_double), ("ms_split", C.c_double),
                 ("ms_gemm", C.c_double), ("n_cblocks", C.c_longlong),
                 ("n_pairs", C.c_longlong), ("slice_bytes", C.c_longlong),
-                ("precision_used", C.c_int), ("gemm_launches", C.c_int)]
+                ("precision_used", C.c_int), ("gemm_launches", C.c_int),
+                ("stage_bytes", C.c_longlong), ("stage_batches", C.c_int),
+                ("pad_", C.c_int), ("ms_stage_wait", C.c_double)]
 
 
 _P = C.c_void_p
@@ -124,6 +126,7 @@ _GB_SIGS = {
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
     "xmg_plan_cache_clear": (None, []),
+    "xmg_set_staging": (C.c_int, [C.c_size_t, C.c_size_t]),
     "xm_contract_adjoint": (C.c_int, [Scalar, _P, _P, _P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p]),
     "xmg_timer_start": (C.c_int, []),
     "xmg_timer_stop": (C.c_double, []),

@@ -24,6 +24,13 @@ struct buf { void *p; size_t n; };
 static buf g_scratch[XMGD_SCRATCH_SLOTS];
 static buf g_pinned;
 
+/* staging side stream: host-to-device copies of out-of-core operand
+ * blocks from two pinned chunk buffers, overlapping the compute stream */
+static cudaStream_t g_side = nullptr;
+static cudaEvent_t g_side_ev[2];
+static bool g_side_rec[2];
+static buf g_chunk[2];
+
 cudaStream_t stream() { return g_stream; }
 int num_sms() { return g_sms; }
 
@@ -67,6 +74,9 @@ xmgd_init(void)
 	XMG_CK(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount,
 	    g_dev));
 	XMG_CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+	XMG_CK(cudaStreamCreateWithFlags(&g_side, cudaStreamNonBlocking));
+	for (int i = 0; i < 2; i++)
+		XMG_CK(cudaEventCreateWithFlags(&g_side_ev[i], cudaEventDisableTiming));
 	/* keep freed block memory in the pool: tensors are created and freed
 	 * often and cudaMalloc/cudaFree would synchronise the device */
 	XMG_CK(cudaDeviceGetDefaultMemPool(&pool, g_dev));
@@ -183,6 +193,62 @@ xmgd_pinned(size_t bytes, void **hptr)
 		g_pinned.n = bytes;
 	}
 	*hptr = g_pinned.p;
+	return XMG_OK;
+}
+
+/* make the calling host thread use the engine's device */
+extern "C" int
+xmgd_bind_thread(void)
+{
+	XMG_CK(cudaSetDevice(g_dev));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_side_wait(int slot)
+{
+	if (g_side_rec[slot]) {
+		XMG_CK(cudaEventSynchronize(g_side_ev[slot]));
+		g_side_rec[slot] = false;
+	}
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_side_chunk(int slot, size_t bytes, void **hptr)
+{
+	buf *b = &g_chunk[slot];
+	int st;
+
+	if (b->n < bytes) {
+		if ((st = xmgd_side_wait(slot)) != XMG_OK)
+			return st;
+		if (b->p)
+			XMG_CK(cudaFreeHost(b->p));
+		b->p = nullptr;
+		b->n = 0;
+		XMG_CK(cudaMallocHost(&b->p, bytes));
+		b->n = bytes;
+	}
+	*hptr = b->p;
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_side_copy(int slot, uint64_t dst, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst, g_chunk[slot].p, bytes,
+	    cudaMemcpyHostToDevice, g_side));
+	XMG_CK(cudaEventRecord(g_side_ev[slot], g_side));
+	g_side_rec[slot] = true;
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_side_sync(void)
+{
+	XMG_CK(cudaStreamSynchronize(g_side));
+	g_side_rec[0] = g_side_rec[1] = false;
 	return XMG_OK;
 }
 

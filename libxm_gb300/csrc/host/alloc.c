@@ -31,6 +31,8 @@ struct xm_allocator {
 	unsigned char *used;      /* one bit per page */
 	xmg_hmap_t live;          /* HBM: live handle -> bytes */
 	xmg_hmap_t views;         /* pagefile: handle -> staged device addr */
+	xmg_hmap_t stream;        /* pagefile: handle -> address in the
+	                             current out-of-core batch */
 };
 
 static int bit_get(const unsigned char *b, uint64_t i) { return (b[i >> 3] >> (i & 7)) & 1; }
@@ -54,6 +56,7 @@ xm_allocator_create(const char *path)
 	}
 	xmg_hmap_init(&a->live);
 	xmg_hmap_init(&a->views);
+	xmg_hmap_init(&a->stream);
 	a->fd = -1;
 	if (path == NULL) {
 		if (xmgd_init() != XMG_OK) {
@@ -241,7 +244,8 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 		*dptr = h;
 		return XMG_OK;
 	}
-	if (xmg_hmap_get(&a->views, h, dptr))
+	if (xmg_hmap_get(&a->stream, h, dptr) ||
+	    xmg_hmap_get(&a->views, h, dptr))
 		return XMG_OK;
 	if ((st = xmgd_alloc(bytes, &d)) != XMG_OK)
 		return st;
@@ -293,6 +297,29 @@ xmg_alloc_release_views(xm_allocator_t *a, int write_back)
 	return XMG_OK;
 }
 
+/* Out-of-core batches: while set, blocks of the batch resolve to their
+ * addresses in the staging region instead of whole-block views. */
+int
+xmg_alloc_stream_set(xm_allocator_t *a, const uint64_t *h, const uint64_t *d,
+    size_t n)
+{
+	size_t i;
+
+	xmg_hmap_free(&a->stream);
+	xmg_hmap_init(&a->stream);
+	for (i = 0; i < n; i++)
+		if (xmg_hmap_put(&a->stream, h[i], d[i]))
+			return xmg_seterr(XMG_ENOMEM, "out of memory");
+	return XMG_OK;
+}
+
+void
+xmg_alloc_stream_clear(xm_allocator_t *a)
+{
+	xmg_hmap_free(&a->stream);
+	xmg_hmap_init(&a->stream);
+}
+
 void
 xm_allocator_destroy(xm_allocator_t *a)
 {
@@ -314,6 +341,7 @@ xm_allocator_destroy(xm_allocator_t *a)
 	}
 	xmg_hmap_free(&a->live);
 	xmg_hmap_free(&a->views);
+	xmg_hmap_free(&a->stream);
 	free(a->path);
 	free(a->used);
 	free(a);

@@ -14,6 +14,7 @@
  * precision path and a work list for the grouped GEMM.
  */
 #include <math.h>
+#include <pthread.h>
 #include <time.h>
 
 #include "xmg_host.h"
@@ -163,6 +164,12 @@ typedef struct {
 	double flops;
 	uint8_t *emulatable;     /* per cblock */
 	int capem;
+	/* out-of-core: only pairs whose b data is in bfilter; collect lists
+	 * the b data handles (and bytes) of every surviving pair */
+	const xmg_hmap_t *bfilter;
+	int collect;
+	uint64_t *bh, *bsz;
+	size_t nbh, capbh;
 } plan_t;
 
 #define GROW(arr, n, cap) do {						\
@@ -179,6 +186,8 @@ plan_free(plan_t *p)
 	free(p->cb); free(p->pr); free(p->va); free(p->vb); free(p->tabs.v);
 	free(p->tabs.desc);
 	free(p->emulatable);
+	free(p->bh);
+	free(p->bsz);
 	xmg_hmap_free(&p->tabs.index);
 	xmg_hmap_free(&p->va_index); xmg_hmap_free(&p->vb_index);
 	xmg_hmap_free(&p->ea_index); xmg_hmap_free(&p->eb_index);
@@ -495,6 +504,19 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		for (i = 0; i < nblkk; i++) {
 			if (cand[i].al == 0)
 				continue;
+			if (p->bfilter && !xmg_hmap_get(p->bfilter, cand[i].db, NULL))
+				continue;	/* b block outside this batch */
+			if (p->collect) {
+				if (p->nbh == p->capbh) {
+					p->capbh = p->capbh ? 2 * p->capbh : 256;
+					if ((p->bh = realloc(p->bh, p->capbh *
+					    sizeof *p->bh)) == NULL || (p->bsz =
+					    realloc(p->bsz, p->capbh * sizeof *p->bsz)) == NULL)
+						xm_fatal("%s: out of memory", __func__);
+				}
+				p->bh[p->nbh] = cand[i].db;
+				p->bsz[p->nbh++] = xm_tensor_get_block_bytes(b, cand[i].ib);
+			}
 			dA = xm_block_space_get_block_dims(a->bs, cand[i].ia);
 			dB = xm_block_space_get_block_dims(b->bs, cand[i].ib);
 			GROW(p->pr, p->npr, p->cappr);
@@ -602,6 +624,349 @@ xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
 }
 
 /* ------------------------------------------------------------------ */
+/* out-of-core contraction                                             */
+
+/*
+ * b's pagefile blocks are streamed through two HBM regions: an I/O thread
+ * reads batch i+1 from the pagefile into two pinned 64 MiB chunks in turn
+ * and copies each on the side stream (cudaMemcpyAsync) into the idle region
+ * while batch i is contracted on the compute stream.  Each batch is an
+ * ordinary contraction restricted to the merged pairs whose b data lies in
+ * the batch (pairs merge only over equal b data, so the restriction
+ * commutes with merging); beta is applied by the first batch and the later
+ * ones accumulate with beta = 1.
+ */
+#define STAGE_CHUNK ((size_t)64 << 20)
+#define STAGE_ALIGN 256
+
+static size_t g_stage_budget, g_stage_region;
+
+static size_t
+env_bytes(const char *name, double gb)
+{
+	const char *e = getenv(name);
+
+	return (size_t)((e ? atof(e) : gb) * 1e9);
+}
+
+int
+xmg_set_staging(size_t budget, size_t region)
+{
+	if (budget)
+		g_stage_budget = budget;
+	if (region)
+		g_stage_region = region;
+	return XMG_OK;
+}
+
+struct io_job {
+	xm_allocator_t *al;
+	const uint64_t *h, *sz, *off;
+	size_t n;
+	uint64_t region;
+	int status;
+	char err[256];
+	pthread_t th;
+	int running;
+};
+
+static void *
+io_main(void *arg)
+{
+	struct io_job *j = arg;
+	size_t i, o, n, k = 0;
+	void *buf;
+	int st = xmgd_bind_thread();
+
+	for (i = 0; st == XMG_OK && i < j->n; i++)
+		for (o = 0; st == XMG_OK && o < j->sz[i]; o += n, k++) {
+			const int slot = (int)(k & 1);
+			n = j->sz[i] - o < STAGE_CHUNK ? j->sz[i] - o : STAGE_CHUNK;
+			/* the chunk is refilled only after its previous copy */
+			if ((st = xmgd_side_wait(slot)) == XMG_OK &&
+			    (st = xmgd_side_chunk(slot, STAGE_CHUNK, &buf)) == XMG_OK &&
+			    (st = xmg_alloc_read_range(j->al, j->h[i], o, buf, n)) ==
+			    XMG_OK)
+				st = xmgd_side_copy(slot, j->region + j->off[i] + o, n);
+		}
+	if (xmgd_side_sync() != XMG_OK && st == XMG_OK)
+		st = XMG_ECUDA;
+	j->status = st;
+	if (st != XMG_OK)
+		snprintf(j->err, sizeof j->err, "%s", xmg_last_error());
+	return NULL;
+}
+
+static int
+io_start(struct io_job *j)
+{
+	j->status = XMG_OK;
+	j->err[0] = '\0';
+	if (pthread_create(&j->th, NULL, io_main, j))
+		return xmg_seterr(XMG_ENOMEM, "cannot start the staging thread");
+	j->running = 1;
+	return XMG_OK;
+}
+
+static int
+io_join(struct io_job *j)
+{
+	if (!j->running)
+		return XMG_OK;
+	pthread_join(j->th, NULL);
+	j->running = 0;
+	if (j->status != XMG_OK)
+		return xmg_seterr(j->status, "staging: %s", j->err);
+	return XMG_OK;
+}
+
+struct hsz {
+	uint64_t h, sz;
+};
+
+static int
+cmp_hsz(const void *x, const void *y)
+{
+	const struct hsz *p = x, *q = y;
+
+	return p->h < q->h ? -1 : p->h > q->h;
+}
+
+static void
+fill_contract(xmgd_contract_t *dp, const plan_t *p, xm_scalar_t alpha,
+    xm_scalar_t beta, int prec)
+{
+	memset(dp, 0, sizeof *dp);
+	dp->dtype = p->type;
+	dp->precision = prec;
+	xmg_scalar_pack(alpha, dp->alpha);
+	xmg_scalar_pack(beta, dp->beta);
+	dp->ncblocks = p->ncb;
+	dp->npairs = p->npr;
+	dp->cblocks = p->cb;
+	dp->pairs = p->pr;
+	dp->views_a = p->va;
+	dp->views_b = p->vb;
+	dp->nviews_a = p->nva;
+	dp->nviews_b = p->nvb;
+	dp->tabs = p->tabs.v;
+	dp->ntabs = p->tabs.n;
+	dp->nexp_a = p->nexp_a;
+	dp->nexp_b = p->nexp_b;
+	dp->flops = p->flops;
+	dp->emulatable = p->emulatable;
+}
+
+/* Write c's staged views back to its pagefile and drop every view. */
+static int
+commit_c(xm_tensor_t *c, int st)
+{
+	xm_dim_t *list;
+	size_t n, q;
+
+	if (xmg_alloc_is_device(c->allocator))
+		return st;
+	if (st == XMG_OK) {
+		xm_tensor_get_canonical_block_list(c, &list, &n);
+		for (q = 0; q < n && st == XMG_OK; q++)
+			st = xmg_alloc_commit_view(c->allocator,
+			    xm_tensor_get_block_data_ptr(c, list[q]),
+			    xm_tensor_get_block_bytes(c, list[q]));
+		free(list);
+	}
+	xmg_alloc_release_views(c->allocator, 0);
+	return st;
+}
+
+/*
+ * Out-of-core path.  Returns 0 when the contraction should run in core
+ * (b in GPU memory, b aliasing a or c, or b's blocks within the budget),
+ * else 1 with the status in *st.
+ */
+static int
+contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
+    const xm_tensor_t *b, xm_scalar_t beta, xm_tensor_t *c,
+    const char *idxa, const char *idxb, const char *idxc, int prec, int *st)
+{
+	plan_t p0;
+	struct hsz *u = NULL;
+	uint64_t *H = NULL, *SZ = NULL, *OFF = NULL, *D = NULL, total = 0;
+	uint64_t reg[2] = {0, 0}, rbytes = 0, run;
+	size_t budget, region, nu = 0, i, *bstart = NULL, nb = 0, k;
+	struct io_job io[2];
+	xmg_hmap_t filt;
+	xmg_stats_t acc;
+	double tw;
+	int used_all = XMG_PREC_EMU64;
+
+	if (xmg_alloc_is_device(b->allocator) || b == a || b == c)
+		return 0;
+	if (!g_stage_budget)
+		g_stage_budget = env_bytes("XMG_STAGE_BUDGET_GB", 180);
+	if (!g_stage_region)
+		g_stage_region = env_bytes("XMG_STAGE_REGION_GB", 32);
+	budget = g_stage_budget;
+	region = g_stage_region;
+	init_plan(&p0);
+	p0.collect = 1;
+	if (check_contract(a, b, c, idxa, idxb, idxc, &p0) != XMG_OK ||
+	    build_plan(alpha, a, b, c, &p0, 0) != XMG_OK) {
+		plan_free(&p0);
+		return 0;	/* the in-core path reports it */
+	}
+	/* distinct b blocks in file order */
+	if (p0.nbh && (u = malloc(p0.nbh * sizeof *u)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < p0.nbh; i++) {
+		u[i].h = p0.bh[i];
+		u[i].sz = p0.bsz[i];
+	}
+	qsort(u, p0.nbh, sizeof *u, cmp_hsz);
+	for (i = 0; i < p0.nbh; i++)
+		if (nu == 0 || u[nu - 1].h != u[i].h)
+			u[nu++] = u[i];
+	for (i = 0; i < nu; i++)
+		total += u[i].sz;
+	plan_free(&p0);
+	if (total <= budget) {
+		free(u);
+		return 0;
+	}
+	/* batches of at most `region` bytes (256-byte aligned offsets) */
+	H = malloc(nu * sizeof *H);
+	SZ = malloc(nu * sizeof *SZ);
+	OFF = malloc(nu * sizeof *OFF);
+	D = malloc(nu * sizeof *D);
+	bstart = malloc((nu + 1) * sizeof *bstart);
+	if (!H || !SZ || !OFF || !D || !bstart)
+		xm_fatal("%s: out of memory", __func__);
+	run = 0;
+	for (i = 0; i < nu; i++) {
+		uint64_t al = (u[i].sz + STAGE_ALIGN - 1) / STAGE_ALIGN * STAGE_ALIGN;
+		if (al > region) {
+			*st = xmg_seterr(XMG_ENOMEM, "xm_contract: a block of b "
+			    "(%llu bytes) exceeds the staging region (%zu bytes)",
+			    (unsigned long long)u[i].sz, region);
+			goto out;
+		}
+		if (i == 0 || run + al > region) {
+			bstart[nb++] = i;
+			run = 0;
+		}
+		H[i] = u[i].h;
+		SZ[i] = u[i].sz;
+		OFF[i] = run;
+		run += al;
+		if (run > rbytes)
+			rbytes = run;
+	}
+	bstart[nb] = nu;
+	memset(io, 0, sizeof io);
+	memset(&acc, 0, sizeof acc);
+	xmg_hmap_init(&filt);
+	if ((*st = xmgd_alloc(rbytes, &reg[0])) != XMG_OK ||
+	    (nb > 1 && (*st = xmgd_alloc(rbytes, &reg[1])) != XMG_OK) ||
+	    (*st = xmgd_sync()) != XMG_OK)
+		goto out_free;
+	for (k = 0; k < 2; k++)
+		io[k].al = b->allocator;
+	/* batch 0 first, synchronously */
+	io[0].h = H; io[0].sz = SZ; io[0].off = OFF;
+	io[0].n = bstart[1];
+	io[0].region = reg[0];
+	if ((*st = io_start(&io[0])) != XMG_OK || (*st = io_join(&io[0])) != XMG_OK)
+		goto out_free;
+	tw = 0;
+	for (k = 0; k < nb && *st == XMG_OK; k++) {
+		struct io_job *nx = &io[(k + 1) & 1];
+		xmgd_contract_t dp;
+		xmgd_plan_t *hp = NULL;
+		plan_t p;
+		int used = XMG_PREC_FP64;
+		double t0;
+
+		if (k + 1 < nb) {
+			nx->h = H + bstart[k + 1];
+			nx->sz = SZ + bstart[k + 1];
+			nx->off = OFF + bstart[k + 1];
+			nx->n = bstart[k + 2] - bstart[k + 1];
+			nx->region = reg[(k + 1) & 1];
+			if ((*st = io_start(nx)) != XMG_OK)
+				break;
+		}
+		/* the batch's blocks resolve into its region */
+		xmg_hmap_free(&filt);
+		xmg_hmap_init(&filt);
+		for (i = bstart[k]; i < bstart[k + 1]; i++) {
+			D[i] = reg[k & 1] + OFF[i];
+			xmg_hmap_put(&filt, H[i], 1);
+		}
+		if ((*st = xmg_alloc_stream_set(b->allocator, H + bstart[k],
+		    D + bstart[k], bstart[k + 1] - bstart[k])) != XMG_OK)
+			break;
+		init_plan(&p);
+		p.bfilter = &filt;
+		if ((*st = check_contract(a, b, c, idxa, idxb, idxc, &p)) ==
+		    XMG_OK && (*st = build_plan(alpha, a, b, c, &p, 1)) == XMG_OK) {
+			fill_contract(&dp, &p, alpha, k == 0 ? beta : 1, prec);
+			if ((*st = xmgd_plan_create(&dp, &hp)) == XMG_OK) {
+				*st = xmgd_plan_run(hp, &used);
+				xmgd_plan_free(hp);
+			}
+		}
+		if (*st == XMG_OK) {
+			xmgd_timing_t tm;
+			xmgd_last_timing(&tm);
+			acc.flops += p.flops;
+			acc.ms_device += tm.ms_total;
+			acc.ms_split += tm.ms_split;
+			acc.ms_gemm += tm.ms_gemm;
+			acc.n_pairs += p.npr;
+			acc.gemm_launches += tm.gemm_launches;
+			if (tm.slice_bytes > acc.slice_bytes)
+				acc.slice_bytes = tm.slice_bytes;
+			if (p.npr > 0 && used != XMG_PREC_EMU64)
+				used_all = XMG_PREC_FP64;
+		}
+		plan_free(&p);
+		xmg_alloc_stream_clear(b->allocator);
+		t0 = now_ms();
+		if (k + 1 < nb) {
+			int s2 = io_join(nx);
+			if (*st == XMG_OK)
+				*st = s2;
+		}
+		tw += now_ms() - t0;
+	}
+	for (k = 0; k < 2; k++)
+		io_join(&io[k]);	/* never leave a copy in flight */
+	acc.n_cblocks = 0;
+	{
+		xm_dim_t *list; size_t n;
+		xm_tensor_get_canonical_block_list(c, &list, &n);
+		acc.n_cblocks = (long long)n;
+		free(list);
+	}
+	acc.precision_used = used_all;
+	acc.stage_bytes = (long long)total;
+	acc.stage_batches = (int)nb;
+	acc.ms_stage_wait = tw;
+	g_stats = acc;
+out_free:
+	xmg_alloc_stream_clear(b->allocator);
+	xmg_hmap_free(&filt);
+	if (reg[0])
+		xmgd_free(reg[0]);
+	if (reg[1])
+		xmgd_free(reg[1]);
+	*st = commit_c(c, *st);
+	xmg_alloc_release_views(a->allocator, 0);
+out:
+	free(u); free(H); free(SZ); free(OFF); free(D); free(bstart);
+	return 1;
+}
+
+/* ------------------------------------------------------------------ */
 /* plan cache                                                          */
 
 /*
@@ -704,7 +1069,7 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	struct pc_entry *e = NULL;
 	plan_t p;
 	double t0 = now_ms();
-	int st, l, i, prec = precision_mode(), used = XMG_PREC_FP64, cache;
+	int st, i, prec = precision_mode(), used = XMG_PREC_FP64, cache;
 
 	init_plan(&p);
 	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) != XMG_OK)
@@ -712,6 +1077,9 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	if ((st = xmgd_init()) != XMG_OK)
 		goto out;
 	memset(&g_stats, 0, sizeof g_stats);
+	if (!xmg_alloc_is_device(c->allocator) && contract_streamed(alpha, a, b,
+	    beta, c, idxa, idxb, idxc, prec, &st))
+		goto out;
 	cache = pc_slots() > 0 && xmg_alloc_is_device(c->allocator) &&
 	    strlen(idxa) < 16 && strlen(idxb) < 16 && strlen(idxc) < 16;
 	if (cache) {
@@ -729,29 +1097,15 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			goto out;
 		}
 	}
-	if ((st = build_plan(alpha, a, b, c, &p, 1)) != XMG_OK)
+	if ((st = build_plan(alpha, a, b, c, &p, 1)) != XMG_OK) {
+		st = commit_c(c, st);
 		goto out;
-	memset(&dp, 0, sizeof dp);
-	dp.dtype = c->type;
-	dp.precision = prec;
-	xmg_scalar_pack(alpha, dp.alpha);
-	xmg_scalar_pack(beta, dp.beta);
-	dp.ncblocks = p.ncb;
-	dp.npairs = p.npr;
-	dp.cblocks = p.cb;
-	dp.pairs = p.pr;
-	dp.views_a = p.va;
-	dp.views_b = p.vb;
-	dp.nviews_a = p.nva;
-	dp.nviews_b = p.nvb;
-	dp.tabs = p.tabs.v;
-	dp.ntabs = p.tabs.n;
-	dp.nexp_a = p.nexp_a;
-	dp.nexp_b = p.nexp_b;
-	dp.flops = p.flops;
-	dp.emulatable = p.emulatable;
-	if ((st = xmgd_plan_create(&dp, &h)) != XMG_OK)
+	}
+	fill_contract(&dp, &p, alpha, beta, prec);
+	if ((st = xmgd_plan_create(&dp, &h)) != XMG_OK) {
+		st = commit_c(c, st);
 		goto out;
+	}
 	g_stats.ms_plan = now_ms() - t0;
 	st = xmgd_plan_run(h, &used);
 	stats_from(p.flops, p.ncb, p.npr, used, t0);
@@ -779,19 +1133,7 @@ xmg_contract(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	}
 	if (h)
 		xmgd_plan_free(h);
-	if (st == XMG_OK && !xmg_alloc_is_device(c->allocator)) {
-		for (l = 0; l < p.ncb && st == XMG_OK; l++) {
-			xm_dim_t *list; size_t n;
-			xm_tensor_get_canonical_block_list(c, &list, &n);
-			for (size_t q = 0; q < n && st == XMG_OK; q++)
-				st = xmg_alloc_commit_view(c->allocator,
-				    xm_tensor_get_block_data_ptr(c, list[q]),
-				    xm_tensor_get_block_bytes(c, list[q]));
-			free(list);
-			break;
-		}
-		xmg_alloc_release_views(c->allocator, 0);
-	}
+	st = commit_c(c, st);
 out:
 	plan_free(&p);
 	return st;

@@ -72,6 +72,9 @@ static inline void xmg_scalar_pack(xm_scalar_t s, double out[2])
 int xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
     void *mem, size_t bytes);
 int xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes);
+int xmg_alloc_stream_set(xm_allocator_t *a, const uint64_t *h,
+    const uint64_t *d, size_t n);
+void xmg_alloc_stream_clear(xm_allocator_t *a);
 
 /* Permuted-copy task helpers (blockops.c). */
 /* Normalise an iteration space: drop extent-1 dimensions and merge
