@@ -68,7 +68,8 @@ def build(verbose=False):
             print(msg)
     if _stale(LIB, objs) or _arch_tag() != platform.machine():
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
-            "-lcudart_static", "-ldl", "-lrt", "-lpthread", "-lm"]
+            "-lcudart_static", "-ldl", "-lrt", "-lpthread", "-lm",
+            "-Xlinker", "-z", "-Xlinker", "defs"]   # no undefined symbols
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -27,9 +27,9 @@ static buf g_pinned;
 /* staging side stream: host-to-device copies of out-of-core operand
  * blocks from two pinned chunk buffers, overlapping the compute stream */
 static cudaStream_t g_side = nullptr;
-static cudaEvent_t g_side_ev[2];
-static bool g_side_rec[2];
-static buf g_chunk[2];
+static cudaEvent_t g_side_ev[XMGD_SIDE_SLOTS];
+static bool g_side_rec[XMGD_SIDE_SLOTS];
+static buf g_chunk[XMGD_SIDE_SLOTS];
 
 cudaStream_t stream() { return g_stream; }
 int num_sms() { return g_sms; }
@@ -75,7 +75,7 @@ xmgd_init(void)
 	    g_dev));
 	XMG_CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
 	XMG_CK(cudaStreamCreateWithFlags(&g_side, cudaStreamNonBlocking));
-	for (int i = 0; i < 2; i++)
+	for (int i = 0; i < XMGD_SIDE_SLOTS; i++)
 		XMG_CK(cudaEventCreateWithFlags(&g_side_ev[i], cudaEventDisableTiming));
 	/* keep freed block memory in the pool: tensors are created and freed
 	 * often and cudaMalloc/cudaFree would synchronise the device */
@@ -248,7 +248,8 @@ extern "C" int
 xmgd_side_sync(void)
 {
 	XMG_CK(cudaStreamSynchronize(g_side));
-	g_side_rec[0] = g_side_rec[1] = false;
+	for (int i = 0; i < XMGD_SIDE_SLOTS; i++)
+		g_side_rec[i] = false;
 	return XMG_OK;
 }
 

@@ -627,10 +627,11 @@ xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
 /* out-of-core contraction                                             */
 
 /*
- * b's pagefile blocks are streamed through two HBM regions: an I/O thread
- * reads batch i+1 from the pagefile into two pinned 64 MiB chunks in turn
- * and copies each on the side stream (cudaMemcpyAsync) into the idle region
- * while batch i is contracted on the compute stream.  Each batch is an
+ * b's pagefile blocks are streamed through two HBM regions: reader threads
+ * (XMG_STAGE_THREADS, default 8) read batch i+1 from the pagefile into
+ * pinned 64 MiB chunks, two per reader used in turn, and copy each on the
+ * side stream (cudaMemcpyAsync) into the idle region while batch i is
+ * contracted on the compute stream.  Each batch is an
  * ordinary contraction restricted to the merged pairs whose b data lies in
  * the batch (pairs merge only over equal b data, so the restriction
  * commutes with merging); beta is applied by the first batch and the later
@@ -670,30 +671,85 @@ struct io_job {
 	int running;
 };
 
+/* one reader: chunks w, w + nw, w + 2 nw, ... of the batch, alternating
+ * its two pinned slots */
+struct io_worker {
+	struct io_job *j;
+	int w, nw, status;
+	char err[256];
+};
+
 static void *
-io_main(void *arg)
+io_worker_main(void *arg)
 {
-	struct io_job *j = arg;
-	size_t i, o, n, k = 0;
+	struct io_worker *r = arg;
+	struct io_job *j = r->j;
+	size_t i, o, n, k = 0, mine = 0;
 	void *buf;
 	int st = xmgd_bind_thread();
 
 	for (i = 0; st == XMG_OK && i < j->n; i++)
 		for (o = 0; st == XMG_OK && o < j->sz[i]; o += n, k++) {
-			const int slot = (int)(k & 1);
 			n = j->sz[i] - o < STAGE_CHUNK ? j->sz[i] - o : STAGE_CHUNK;
-			/* the chunk is refilled only after its previous copy */
+			if ((int)(k % (size_t)r->nw) != r->w)
+				continue;
+			const int slot = 2 * r->w + (int)(mine++ & 1);
+			/* a chunk is refilled only after its previous copy */
 			if ((st = xmgd_side_wait(slot)) == XMG_OK &&
 			    (st = xmgd_side_chunk(slot, STAGE_CHUNK, &buf)) == XMG_OK &&
 			    (st = xmg_alloc_read_range(j->al, j->h[i], o, buf, n)) ==
 			    XMG_OK)
 				st = xmgd_side_copy(slot, j->region + j->off[i] + o, n);
 		}
-	if (xmgd_side_sync() != XMG_OK && st == XMG_OK)
-		st = XMG_ECUDA;
-	j->status = st;
+	r->status = st;
 	if (st != XMG_OK)
+		snprintf(r->err, sizeof r->err, "%s", xmg_last_error());
+	return NULL;
+}
+
+static int
+stage_threads(void)
+{
+	const char *e = getenv("XMG_STAGE_THREADS");
+	int n = e ? atoi(e) : 8;
+
+	return n < 1 ? 1 : n > XMGD_SIDE_SLOTS / 2 ? XMGD_SIDE_SLOTS / 2 : n;
+}
+
+static void *
+io_main(void *arg)
+{
+	struct io_job *j = arg;
+	struct io_worker r[XMGD_SIDE_SLOTS / 2];
+	pthread_t th[XMGD_SIDE_SLOTS / 2];
+	int nw = stage_threads(), w, started = 0, st = XMG_OK;
+
+	for (w = 0; w < nw; w++) {
+		r[w].j = j;
+		r[w].w = w;
+		r[w].nw = nw;
+		r[w].status = XMG_OK;
+		r[w].err[0] = '\0';
+	}
+	for (w = 0; w < nw; w++, started++)
+		if (pthread_create(&th[w], NULL, io_worker_main, &r[w])) {
+			st = XMG_ENOMEM;
+			snprintf(j->err, sizeof j->err, "cannot start a reader");
+			break;
+		}
+	for (w = 0; w < started; w++) {
+		pthread_join(th[w], NULL);
+		if (r[w].status != XMG_OK && st == XMG_OK) {
+			st = r[w].status;
+			snprintf(j->err, sizeof j->err, "%s", r[w].err);
+		}
+	}
+	xmgd_bind_thread();
+	if (xmgd_side_sync() != XMG_OK && st == XMG_OK) {
+		st = XMG_ECUDA;
 		snprintf(j->err, sizeof j->err, "%s", xmg_last_error());
+	}
+	j->status = st;
 	return NULL;
 }
 

@@ -26,10 +26,12 @@ int xmgd_is_device_ptr(const void *p);
 int xmgd_scratch(int slot, size_t bytes, uint64_t *dptr);
 /* Pinned host staging buffer (grow-only). */
 int xmgd_pinned(size_t bytes, void **hptr);
-/* Out-of-core staging on the side stream: two pinned chunk buffers
- * (slot 0/1); side_copy sends chunk `slot` to dst asynchronously,
- * side_wait blocks until that slot's last copy is done (the buffer may
- * then be refilled), side_sync drains the side stream. */
+/* Out-of-core staging on the side stream: pinned chunk buffers in
+ * XMGD_SIDE_SLOTS slots (two per reader thread); side_copy sends chunk
+ * `slot` to dst asynchronously, side_wait blocks until that slot's last
+ * copy is done (the buffer may then be refilled), side_sync drains the
+ * side stream.  Distinct slots may be used from distinct threads. */
+#define XMGD_SIDE_SLOTS 16
 int xmgd_bind_thread(void);
 int xmgd_side_chunk(int slot, size_t bytes, void **hptr);
 int xmgd_side_copy(int slot, uint64_t dst, size_t bytes);
