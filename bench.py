@@ -45,6 +45,10 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-out-of-core", action="store_true",
+                   help="skip the pagefile-streamed measurement")
+    p.add_argument("--no-elementwise", action="store_true",
+                   help="skip the xm_set / xm_add bandwidth measurement")
     p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
     p.add_argument("--subset", type=str, default=None,
                    help="O,V: keep the first O occupied and V virtual blocks (profiling case)")
@@ -221,6 +225,11 @@ def block_costs(w):
     return cost
 
 
+# DRAM bytes (read + write) of one split-precision GEMM launch on the cfg2
+# ladder, from a single-pass ncu capture of that kernel on this workload
+GEMM_DRAM_BYTES = 127.71e9 + 0.74062e9
+
+
 def make_workload(lib, al, scale=1, subset=None):
     from libxm_gb300 import workloads as W
     ob, vb = (int(x) for x in subset.split(",")) if subset else (None, None)
@@ -328,14 +337,78 @@ def engine_arm(args, ranks):
         for p, _ in outs.values():
             eng.xmg_host_free(p)
 
+    # out-of-core: the same contraction with every tensor in a host pagefile
+    # and b streamed through two 2 GB HBM regions (reader threads, pinned
+    # chunks, side-stream copies overlapping the previous batch)
+    ooc = None
+    if not args.no_out_of_core and ranks.rank == 0:
+        import tempfile
+        tmp = tempfile.mkdtemp(prefix="xmg_bench_")
+        pal = api.Allocator(eng, os.path.join(tmp, "pagefile"))
+        wp = make_workload(eng, pal, args.scale, args.subset)
+        eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+        eng.check(eng.xmg_set_staging(1, int(2e9)))
+        wp.run()
+        times = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            wp.run()
+            times.append(time.perf_counter() - t0)
+        st = api.last_stats(eng)
+        dt = min(times)
+        ooc = {"value": flops / dt / 1e12, "unit": "TFLOP/s", "ms_per_step": dt * 1e3,
+               "staged_bytes": st.stage_bytes, "stage_gbs": st.stage_bytes / dt / 1e9,
+               "batches": st.stage_batches, "region_bytes": int(2e9),
+               "device_ms": st.ms_device, "stage_wait_ms": st.ms_stage_wait,
+               "precision_used": "emu64" if st.precision_used == api.PREC_EMU64 else "fp64",
+               "note": "all tensors in a pagefile on the box's disk (page cache warm); "
+                       "b streamed in batches, wall clock per xm_contract"}
+        eng.check(eng.xmg_set_staging(int(180e9), int(32e9)))
+        wp.free()
+        pal.destroy()
+        os.rmdir(tmp)
+
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+
+    # bandwidth-bound operations on b (the largest tensor), timed on the
+    # device through the public calls: xm_set (write), xm_add without and
+    # with a permutation (read a, read b, write a: the gather-transpose
+    # path of unfold/fold)
+    elem = None
+    if not args.no_elementwise:
+        nbytes = sum(w.b.block_size(blk) for blk in w.b.canonical_blocks()) * 8
+        b2 = w.b.structure()
+        api.set_all(b2, 0.25)
+        elem = {}
+        for name, fn, traffic in (
+                ("xm_set", lambda: api.set_all(b2, 1.5), nbytes),
+                ("xm_add", lambda: api.add(0.5, b2, 0.25, w.b, "cdab", "cdab"), 3 * nbytes),
+                ("xm_add_permuted", lambda: api.add(0.5, b2, 0.25, w.b, "cdab", "dcab"), 3 * nbytes)):
+            fn()
+            eng.check(eng.xmg_synchronize())
+            eng.check(eng.xmg_timer_start())
+            reps = 5
+            for _ in range(reps):
+                fn()
+            ms = eng.xmg_timer_stop() / reps
+            gbs = traffic / (ms * 1e-3) / 1e9
+            elem[name] = {"ms": ms, "bytes": traffic, "gbs": gbs, "frac_of_hbm": gbs / hbm_peak}
+        elem["note"] = ("algorithmic bytes of the canonical blocks of b (%.2f GB) per call; "
+                        "device time of the public call, host planning included; peak = "
+                        "measured copy bandwidth" % (nbytes / 1e9))
+        b2.free()
     tc_peak = peaks.get("bf16_tflops", 1900.0)
     slices = 6
     products = slices * (slices + 1) // 2
     if emu["precision_used"] == api.PREC_EMU64 and emu["gemm_ms"] > 0:
         achieved = flops * products / (emu["gemm_ms"] * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
-                "frac": achieved / tc_peak, "traffic": None,
+                "frac": achieved / tc_peak,
+                "traffic": GEMM_DRAM_BYTES if w.name == "cfg2_ladder_o96_v384_z2" else None,
+                "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one emu_gemm "
+                                "launch on this workload (ncu, one pass); the slices and c it "
+                                "must touch are ~13 GB, the rest is L2 misses on re-read tiles",
                 "kernel": "emu_gemm (bf16 slices, tcgen05)",
                 "note": "achieved = useful FP64 flops x %d slice products / mean GEMM-kernel time; peak = measured cuBLAS bf16 burst" % products}
     else:
@@ -369,7 +442,8 @@ def engine_arm(args, ranks):
                     "gpu_fp64_vs_cpu_fp64_sample": rel_fp64_vs_cpu if cpu else None},
         "precision_used": "emu64" if emu["precision_used"] == api.PREC_EMU64 else "fp64",
         "phases_ms": {"gemm": emu["gemm_ms"], "split": emu["split_ms"]},
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "out_of_core": ooc,
+        "elementwise": elem,
         "gpu_launches": emu["launches"], "clocks": emu["clocks"],
         "setup_s": setup_s,
     }

@@ -67,9 +67,8 @@ struct xmgd_plan {
 	std::vector<xmgd_pair_t> prs;
 	std::vector<int> emu, plain;
 	uint64_t d_cbs = 0, d_prs = 0, d_tabs = 0;
-	uint64_t d_scale = 0;                /* staged beta-only tasks */
+	xmgd_ptask_batch_t scale = {};       /* staged beta-only tasks */
 	int n_scale = 0;
-	int64_t scale_ctas = 0;
 	uint64_t d_pg = 0;                   /* plain GEMM work list */
 	int n_pg = 0;
 	emu_plan *ep = nullptr;
@@ -146,7 +145,7 @@ record(xmgd_plan *dp, int seg)
 	switch (seg) {
 	case 0:
 		if (dp->n_scale && (st = xmgd_ptask_launch(dp->dtype, dp->dtype,
-		    dp->d_scale, dp->n_scale, dp->scale_ctas)))
+		    &dp->scale)))
 			return st;
 		return dp->ep ? emu_record_split(dp->ep) : XMG_OK;
 	case 1:
@@ -191,7 +190,7 @@ xmgd_plan_free(xmgd_plan *dp)
 	cudaStreamSynchronize(stream());
 	drop_graphs(dp);
 	emu_free(dp->ep);
-	uint64_t bufs[] = {dp->d_cbs, dp->d_prs, dp->d_tabs, dp->d_scale, dp->d_pg};
+	uint64_t bufs[] = {dp->d_cbs, dp->d_prs, dp->d_tabs, dp->scale.dbuf, dp->d_pg};
 	for (uint64_t b : bufs)
 		if (b)
 			xmgd_free(b);
@@ -264,8 +263,8 @@ xmgd_plan_create(const xmgd_contract_t *p, xmgd_plan **out)
 	}
 	if (!scale.empty()) {
 		dp->n_scale = (int)scale.size();
-		if ((st = xmgd_ptask_stage(scale.data(), dp->n_scale, &dp->d_scale,
-		    &dp->scale_ctas)))
+		if ((st = xmgd_ptask_stage(scale.data(), dp->n_scale, dp->dtype,
+		    &dp->scale)))
 			goto fail;
 	}
 	if (!dp->emu.empty()) {

@@ -9,13 +9,19 @@
  * unfold -> scale -> fold -> axpy host loops (tensor.c:436-639,
  * scalar.c:123-239, xm.c:28-508) with one HBM pass.
  *
- * Two schedules, chosen per task on the host (xmg_ptask_shape):
- *  - row mode: dimension 0 is unit-stride on the destination side; a CTA
- *    covers ROW_ELEMS elements along dim 0 for as many outer rows as fit,
- *    with per-row outer offsets precomputed in shared memory;
- *  - tile mode: the source's unit-stride dimension is dim 1; a CTA moves a
- *    TILE x TILE tile through padded shared memory so that loads are
- *    coalesced along dim 1 and stores along dim 0 (gather-transpose).
+ * Four schedules, chosen per task on the host after xmg_ptask_shape has
+ * normalised the iteration space; each schedule is its own kernel
+ * instantiation (so the lean ones keep few registers and full occupancy),
+ * and a batch launches one kernel per schedule present:
+ *  - flat: one contiguous run on both sides (whole canonical blocks);
+ *  - row: dimension 0 unit-stride on the destination side; a CTA covers
+ *    ROW_ELEMS elements along dim 0 for as many outer rows as fit, with
+ *    per-row outer offsets precomputed in shared memory;
+ *  - matrix: the source's unit-stride dimension is dim 1 and both extents
+ *    fit one tile; a CTA moves whole s0 x s1 slices through padded shared
+ *    memory (loads along the source's runs, stores along the
+ *    destination's): the gather-transpose of unfold/fold;
+ *  - tile: the same for larger extents, TILE x TILE tiles.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -26,12 +32,16 @@
 namespace xmg {
 
 constexpr int PT_THREADS = 256;
-constexpr int ROW_ELEMS = 1024;    /* elements per CTA in row mode */
+constexpr int ROW_ELEMS = 4096;    /* elements per CTA in row mode */
+constexpr int FLAT_ELEMS = 8192;   /* elements per CTA in flat mode */
 constexpr int TILE = 32;
+/* matrix mode: whole s0 x s1 slices (both <= MT) per CTA */
+template <typename S> struct mt_of { static constexpr int v = sizeof(S) <= 8 ? 64 : 32; };
+constexpr int MAT_MAXQ = 64;       /* slices per CTA at most */
 
 struct task_meta {
 	int64_t first_cta;
-	int32_t mode;          /* 0 row, 1 tile */
+	int32_t mode;          /* 0 row, 1 tile, 2 flat, 3 matrix */
 	int32_t rows_per_cta;  /* row mode: outer rows per CTA */
 	int64_t nouter;        /* row: product of dims 1..; tile: dims 2.. */
 	int32_t ctas_d0, ctas_d1;
@@ -88,18 +98,16 @@ outer_offsets(const xmgd_ptask_t &t, int first_dim, int64_t o, int64_t &od,
 	}
 }
 
-template <typename D, typename S>
+template <typename D, typename S, int MODE>
 __global__ void __launch_bounds__(PT_THREADS)
 ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
-    const task_meta *__restrict__ meta, int ntasks, double *__restrict__ partial)
+    const task_meta *__restrict__ meta, int ntasks, int64_t cta0,
+    double *__restrict__ partial)
 {
-	__shared__ int64_t s_od[PT_THREADS], s_os[PT_THREADS];
-	__shared__ __align__(16) char s_tile_raw[TILE * (TILE + 1) * sizeof(S)];
 	__shared__ double s_red[2][PT_THREADS / 32];
-	S (*tile)[TILE + 1] = reinterpret_cast<S (*)[TILE + 1]>(s_tile_raw);
 
 	/* locate the task of this CTA (binary search over first_cta) */
-	int64_t cta = blockIdx.x;
+	const int64_t cta = cta0 + blockIdx.x;
 	int lo = 0, hi = ntasks - 1;
 	while (lo < hi) {
 		int mid = (lo + hi + 1) >> 1;
@@ -115,8 +123,45 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 	const int op = t.op;
 	double dre = 0, dim_ = 0;
 
-	if (m.mode == 0) {
-		/* row mode */
+	if constexpr (MODE == 2) {
+		/* flat: consecutive threads take consecutive elements, four
+		 * loads in flight each, the op resolved outside the loop */
+		const int64_t base = local * FLAT_ELEMS;
+		const int n = (int)(t.size[0] - base < FLAT_ELEMS ? t.size[0] - base :
+		    FLAT_ELEMS);
+		D *dp = dst + base;
+		const S *sp = src + base;
+		switch (op) {
+		case XMGD_OP_SET:
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS)
+				dp[e] = al;
+			break;
+		case XMGD_OP_SCALE:
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS)
+				dp[e] = num<D>::mul(al, dp[e]);
+			break;
+		case XMGD_OP_AXPY:
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS) {
+				const D x = conv<D, S>(sp[e]);
+				dp[e] = num<D>::add(num<D>::mul(al, dp[e]), num<D>::mul(be, x));
+			}
+			break;
+		case XMGD_OP_COPY:
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS)
+				dp[e] = conv<D, S>(num<S>::mul(als, sp[e]));
+			break;
+		default:
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS)
+				elem_op<D, S>::apply(op, dp + e, sp + e, al, als, be, dre, dim_);
+		}
+	} else if constexpr (MODE == 0) {
+		/* row */
+		__shared__ int64_t s_od[PT_THREADS], s_os[PT_THREADS];
 		int64_t s0 = t.size[0];
 		int64_t c0 = local % m.ctas_d0;
 		int64_t orow = (local / m.ctas_d0) * m.rows_per_cta;
@@ -128,17 +173,90 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		for (int r = threadIdx.x; r < rows; r += PT_THREADS)
 			outer_offsets(t, 1, orow + r, s_od[r], s_os[r]);
 		__syncthreads();
-		int64_t n = w0 * rows;
-		int64_t ds0 = t.dst_stride[0], ss0 = t.src_stride[0];
-		for (int64_t e = threadIdx.x; e < n; e += PT_THREADS) {
-			int r = (int)(e / w0);
-			int64_t i0 = i0beg + (e - (int64_t)r * w0);
-			D *dp = dst + s_od[r] + i0 * ds0;
-			const S *sp = src + s_os[r] + i0 * ss0;
-			elem_op<D, S>::apply(op, dp, sp, al, als, be, dre, dim_);
+		const int64_t ds0 = t.dst_stride[0], ss0 = t.src_stride[0];
+		if (w0 >= 32) {
+			/* long rows: wpr warps per row (all eight on one row), lanes
+			 * along it */
+			const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+			const int wpr = rows >= PT_THREADS / 32 ? 1 : (PT_THREADS / 32) / rows;
+			const int step = 32 * wpr;
+			for (int r = warp / wpr; r < rows; r += (PT_THREADS / 32) / wpr) {
+				D *dr = dst + s_od[r];
+				const S *sr = src + s_os[r];
+#pragma unroll 4
+				for (int64_t i0 = i0beg + (warp % wpr) * 32 + lane;
+				    i0 < i0beg + w0; i0 += step)
+					elem_op<D, S>::apply(op, dr + i0 * ds0, sr + i0 * ss0, al,
+					    als, be, dre, dim_);
+			}
+		} else {
+			/* short rows: flattened, 32-bit index arithmetic */
+			const int w0i = (int)w0, n = w0i * rows;
+#pragma unroll 4
+			for (int e = threadIdx.x; e < n; e += PT_THREADS) {
+				const int r = e / w0i;
+				const int64_t i0 = i0beg + (e - r * w0i);
+				elem_op<D, S>::apply(op, dst + s_od[r] + i0 * ds0,
+				    src + s_os[r] + i0 * ss0, al, als, be, dre, dim_);
+			}
+		}
+	} else if constexpr (MODE == 3) {
+		/* matrix: whole s0 x s1 slices (dim 0 unit-stride in dst, dim 1
+		 * in src); rows_per_cta slices per CTA, packed in shared memory
+		 * with row pitch s0 + 1 and moved together: all loads of the
+		 * group in flight, then all stores */
+		constexpr int MT = mt_of<S>::v;
+		__shared__ S mtile[MT * (MT + 1)];
+		__shared__ int64_t s_o[2][MAT_MAXQ];
+		const int s0 = (int)t.size[0], s1 = (int)t.size[1], n = s0 * s1;
+		const int ld = s0 + 1, pitch = s1 * ld;
+		const int64_t ss0 = t.src_stride[0], ds1 = t.dst_stride[1];
+		const int64_t o0 = local * m.rows_per_cta;
+		const int k = (int)(m.nouter - o0 < m.rows_per_cta ? m.nouter - o0 :
+		    m.rows_per_cta);
+		for (int q = threadIdx.x; q < k; q += PT_THREADS)
+			outer_offsets(t, 2, o0 + q, s_o[0][q], s_o[1][q]);
+		__syncthreads();
+		const int kn = k * n;
+		/* flattened walks with the mixed-radix digits advanced by the
+		 * thread stride (one division per CTA, not per element) */
+		{
+			/* loads: e = q n + i0 s1 + i1 (source runs along i1) */
+			int q = threadIdx.x / n, r = threadIdx.x - q * n;
+			int i0 = r / s1, i1 = r - i0 * s1;
+			const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
+			const int d0 = dr / s1, d1 = dr - d0 * s1;
+#pragma unroll 4
+			for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
+				mtile[q * pitch + i1 * ld + i0] = src[s_o[1][q] + i0 * ss0 + i1];
+				i1 += d1;
+				if (i1 >= s1) { i1 -= s1; i0++; }
+				i0 += d0;
+				if (i0 >= s0) { i0 -= s0; q++; }
+				q += dq;
+			}
+		}
+		__syncthreads();
+		{
+			/* stores: e = q n + i1 s0 + i0 (destination runs along i0) */
+			int q = threadIdx.x / n, r = threadIdx.x - q * n;
+			int i1 = r / s0, i0 = r - i1 * s0;
+			const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
+			const int d1 = dr / s0, d0 = dr - d1 * s0;
+#pragma unroll 4
+			for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
+				elem_op<D, S>::apply(op, dst + s_o[0][q] + i0 + i1 * ds1,
+				    &mtile[q * pitch + i1 * ld + i0], al, als, be, dre, dim_);
+				i0 += d0;
+				if (i0 >= s0) { i0 -= s0; i1++; }
+				i1 += d1;
+				if (i1 >= s1) { i1 -= s1; q++; }
+				q += dq;
+			}
 		}
 	} else {
-		/* tile mode: dims 0 (dst unit stride) and 1 (src unit stride) */
+		/* tile: dims 0 (dst unit stride) and 1 (src unit stride) */
+		__shared__ S tile[TILE][TILE + 1];
 		int64_t c0 = local % m.ctas_d0;
 		int64_t rest = local / m.ctas_d0;
 		int64_t c1 = rest % m.ctas_d1;
@@ -148,15 +266,12 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		int64_t b0 = c0 * TILE, b1 = c1 * TILE;
 		int w0 = (int)(t.size[0] - b0 < TILE ? t.size[0] - b0 : TILE);
 		int w1 = (int)(t.size[1] - b1 < TILE ? t.size[1] - b1 : TILE);
-		const bool need_src = op != XMGD_OP_SET && op != XMGD_OP_SCALE;
-		if (need_src) {
-			/* load: consecutive threads walk dim 1 (source contiguous) */
-			for (int e = threadIdx.x; e < TILE * TILE; e += PT_THREADS) {
-				int i1 = e % TILE, i0 = e / TILE;
-				if (i0 < w0 && i1 < w1)
-					tile[i1][i0] = src[os + (b0 + i0) * t.src_stride[0] +
-					    (b1 + i1)];
-			}
+		/* load: consecutive threads walk dim 1 (source contiguous) */
+		for (int e = threadIdx.x; e < TILE * TILE; e += PT_THREADS) {
+			int i1 = e % TILE, i0 = e / TILE;
+			if (i0 < w0 && i1 < w1)
+				tile[i1][i0] = src[os + (b0 + i0) * t.src_stride[0] +
+				    (b1 + i1)];
 		}
 		__syncthreads();
 		/* store: consecutive threads walk dim 0 (destination contiguous) */
@@ -195,36 +310,86 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 template <typename D, typename S>
 static int
 launch(const xmgd_ptask_t *dtasks, const task_meta *dmeta, int ntasks,
-    int64_t nctas, double *dpartial)
+    const int64_t *begin, double *dpartial)
 {
-	/* grid.x limit is 2^31-1; batches are far smaller */
-	ptask_kernel<D, S><<<(unsigned)nctas, PT_THREADS, 0, stream()>>>(
-	    dtasks, dmeta, ntasks, dpartial);
-	g_launches++;
-	return check(cudaGetLastError(), "ptask_kernel launch");
+	/* one launch per schedule, over that schedule's CTA range */
+	for (int mode = 0; mode < 4; mode++) {
+		const int64_t n = begin[mode + 1] - begin[mode];
+		if (n <= 0)
+			continue;
+		switch (mode) {
+		case 0: ptask_kernel<D, S, 0><<<(unsigned)n, PT_THREADS, 0, stream()>>>(
+		    dtasks, dmeta, ntasks, begin[mode], dpartial); break;
+		case 1: ptask_kernel<D, S, 1><<<(unsigned)n, PT_THREADS, 0, stream()>>>(
+		    dtasks, dmeta, ntasks, begin[mode], dpartial); break;
+		case 2: ptask_kernel<D, S, 2><<<(unsigned)n, PT_THREADS, 0, stream()>>>(
+		    dtasks, dmeta, ntasks, begin[mode], dpartial); break;
+		case 3: ptask_kernel<D, S, 3><<<(unsigned)n, PT_THREADS, 0, stream()>>>(
+		    dtasks, dmeta, ntasks, begin[mode], dpartial); break;
+		}
+		g_launches++;
+		XMG_CK(cudaGetLastError());
+	}
+	return XMG_OK;
 }
 
-/* CTA schedule of every task of a batch; returns the grid size */
-static int64_t
-plan_tasks(const xmgd_ptask_t *tasks, int ntasks, task_meta *meta)
+static int
+elem_bytes(int type)
 {
-	int64_t nctas = 0;
+	return type == 0 ? 4 : type == 3 ? 16 : 8;	/* float, cd; double, cf */
+}
+
+/*
+ * Schedule of every task of a batch.  Tasks are grouped by schedule (stable
+ * within a group, order[] maps group position -> caller's index) so that
+ * each schedule owns one contiguous CTA range [begin[m], begin[m+1]); meta
+ * and the task copy follow the grouped order.
+ */
+static void
+plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int stype,
+    std::vector<xmgd_ptask_t> &sorted, std::vector<task_meta> &meta,
+    std::vector<int> &order, int64_t begin[5])
+{
+	std::vector<task_meta> m0((size_t)ntasks);
+	std::vector<int64_t> cnt((size_t)ntasks);
+	const int mt = elem_bytes(stype) <= 8 ? 64 : 32;
 
 	for (int i = 0; i < ntasks; i++) {
 		const xmgd_ptask_t &t = tasks[i];
-		task_meta &m = meta[i];
-		m.first_cta = nctas;
-		bool tile = t.ndim >= 2 && t.src_stride[1] == 1 &&
-		    t.src_stride[0] != 1 && t.op != XMGD_OP_SET &&
-		    t.op != XMGD_OP_SCALE;
-		if (tile) {
+		task_meta &m = m0[i];
+		memset(&m, 0, sizeof m);
+		const bool nosrc = t.op == XMGD_OP_SET || t.op == XMGD_OP_SCALE;
+		const bool tile = t.ndim >= 2 && t.src_stride[1] == 1 &&
+		    t.src_stride[0] != 1 && !nosrc;
+		const bool flat = t.ndim == 1 && t.dst_stride[0] == 1 &&
+		    (nosrc || t.src_stride[0] == 1);
+		const bool mat = tile && t.dst_stride[0] == 1 && t.size[0] <= mt &&
+		    t.size[1] <= mt;
+		if (flat) {
+			m.mode = 2;
+			m.ctas_d0 = (int32_t)((t.size[0] + FLAT_ELEMS - 1) / FLAT_ELEMS);
+			m.nouter = 1;
+			m.rows_per_cta = 1;
+			cnt[i] = m.ctas_d0;
+		} else if (mat) {
+			m.mode = 3;
+			m.nouter = 1;
+			for (int d = 2; d < t.ndim; d++)
+				m.nouter *= t.size[d];
+			/* as many slices as the shared tile holds (pitch s0 + 1) */
+			const int64_t per = t.size[1] * (t.size[0] + 1);
+			int64_t q = (int64_t)mt * (mt + 1) / per;
+			m.rows_per_cta = (int32_t)(q < 1 ? 1 : q > MAT_MAXQ ? MAT_MAXQ : q);
+			m.ctas_d0 = 1;
+			cnt[i] = (m.nouter + m.rows_per_cta - 1) / m.rows_per_cta;
+		} else if (tile) {
 			m.mode = 1;
 			m.ctas_d0 = (t.size[0] + TILE - 1) / TILE;
 			m.ctas_d1 = (t.size[1] + TILE - 1) / TILE;
 			m.nouter = 1;
 			for (int d = 2; d < t.ndim; d++)
 				m.nouter *= t.size[d];
-			nctas += (int64_t)m.ctas_d0 * m.ctas_d1 * m.nouter;
+			cnt[i] = (int64_t)m.ctas_d0 * m.ctas_d1 * m.nouter;
 		} else {
 			m.mode = 0;
 			m.ctas_d0 = (t.size[0] + ROW_ELEMS - 1) / ROW_ELEMS;
@@ -236,20 +401,35 @@ plan_tasks(const xmgd_ptask_t *tasks, int ntasks, task_meta *meta)
 			if (rows > PT_THREADS)
 				rows = PT_THREADS;
 			m.rows_per_cta = (int32_t)rows;
-			nctas += (int64_t)m.ctas_d0 *
-			    ((m.nouter + rows - 1) / rows);
+			cnt[i] = (int64_t)m.ctas_d0 * ((m.nouter + rows - 1) / rows);
 		}
 	}
-	return nctas;
+	sorted.clear();
+	meta.clear();
+	order.clear();
+	int64_t n = 0;
+	for (int mode = 0; mode < 4; mode++) {
+		begin[mode] = n;
+		for (int i = 0; i < ntasks; i++)
+			if (m0[i].mode == mode) {
+				task_meta m = m0[i];
+				m.first_cta = n;
+				n += cnt[i];
+				sorted.push_back(tasks[i]);
+				meta.push_back(m);
+				order.push_back(i);
+			}
+	}
+	begin[4] = n;
 }
 
 static int
 launch_types(int dtype, int stype, const xmgd_ptask_t *dt, const task_meta *dm,
-    int ntasks, int64_t nctas, double *dp)
+    int ntasks, const int64_t *begin, double *dp)
 {
 	int st;
 
-#define L(D, S) st = launch<D, S>(dt, dm, ntasks, nctas, dp)
+#define L(D, S) st = launch<D, S>(dt, dm, ntasks, begin, dp)
 	if (dtype == stype) {
 		switch (dtype) {
 		case 0: L(float, float); break;
@@ -278,96 +458,88 @@ task_bytes(int ntasks)
 using namespace xmg;
 
 extern "C" int
-xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, uint64_t *dbuf,
-    int64_t *nctas)
+xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, int stype,
+    xmgd_ptask_batch_t *b)
 {
-	std::vector<task_meta> meta((size_t)ntasks);
+	std::vector<xmgd_ptask_t> sorted;
+	std::vector<task_meta> meta;
+	std::vector<int> order;
 	const size_t tb = task_bytes(ntasks);
 	int st;
 
-	*dbuf = 0;
-	*nctas = plan_tasks(tasks, ntasks, meta.data());
-	if ((st = xmgd_alloc(tb + meta.size() * sizeof(task_meta), dbuf)))
+	memset(b, 0, sizeof *b);
+	if (ntasks <= 0)
+		return XMG_OK;
+	plan_tasks(tasks, ntasks, stype, sorted, meta, order, b->begin);
+	if ((st = xmgd_alloc(tb + meta.size() * sizeof(task_meta), &b->dbuf)))
 		return st;
-	XMG_CK(cudaMemcpyAsync((void *)*dbuf, tasks, (size_t)ntasks *
+	b->ntasks = ntasks;
+	XMG_CK(cudaMemcpyAsync((void *)b->dbuf, sorted.data(), (size_t)ntasks *
 	    sizeof(xmgd_ptask_t), cudaMemcpyHostToDevice, stream()));
-	XMG_CK(cudaMemcpyAsync((void *)(*dbuf + tb), meta.data(), meta.size() *
+	XMG_CK(cudaMemcpyAsync((void *)(b->dbuf + tb), meta.data(), meta.size() *
 	    sizeof(task_meta), cudaMemcpyHostToDevice, stream()));
-	/* the host copies are the caller's: finish before returning */
+	/* the host copies are local: finish before returning */
 	XMG_CK(cudaStreamSynchronize(stream()));
 	return XMG_OK;
 }
 
 extern "C" int
-xmgd_ptask_launch(int dtype, int stype, uint64_t dbuf, int ntasks,
-    int64_t nctas)
+xmgd_ptask_launch(int dtype, int stype, const xmgd_ptask_batch_t *b)
 {
-	if (ntasks <= 0)
+	if (b->ntasks <= 0)
 		return XMG_OK;
-	return launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
-	    (const task_meta *)(dbuf + task_bytes(ntasks)), ntasks, nctas,
-	    nullptr);
+	return launch_types(dtype, stype, (const xmgd_ptask_t *)b->dbuf,
+	    (const task_meta *)(b->dbuf + task_bytes(b->ntasks)), b->ntasks,
+	    b->begin, nullptr);
 }
 
 extern "C" int
 xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
     double *dots)
 {
-	task_meta *meta;
-	int64_t nctas = 0;
+	std::vector<xmgd_ptask_t> sorted;
+	std::vector<task_meta> meta;
+	std::vector<int> order;
+	int64_t begin[5], nctas;
 	uint64_t dbuf, dpart = 0;
-	size_t tb, mb, k;
-	int st, has_dot = dots != nullptr;
+	size_t tb, mb;
+	int st;
 
 	if (ntasks <= 0)
 		return XMG_OK;
-	if ((meta = (task_meta *)calloc((size_t)ntasks, sizeof *meta)) == NULL)
-		return xmg_seterr(XMG_ENOMEM, "out of memory");
-	nctas = plan_tasks(tasks, ntasks, meta);
-	tb = (size_t)ntasks * sizeof(xmgd_ptask_t);
+	plan_tasks(tasks, ntasks, stype, sorted, meta, order, begin);
+	nctas = begin[4];
+	tb = task_bytes(ntasks);
 	mb = (size_t)ntasks * sizeof(task_meta);
-	tb = (tb + 255) & ~(size_t)255;
 	if ((st = xmgd_scratch(2, tb + mb, &dbuf)) != XMG_OK)
-		goto out;
-	if ((st = check(cudaMemcpyAsync((void *)dbuf, tasks, (size_t)ntasks *
-	    sizeof(xmgd_ptask_t), cudaMemcpyHostToDevice, stream()),
-	    "task upload")) != XMG_OK)
-		goto out;
-	if ((st = check(cudaMemcpyAsync((void *)(dbuf + tb), meta, mb,
-	    cudaMemcpyHostToDevice, stream()), "task upload")) != XMG_OK)
-		goto out;
-	if (has_dot && (st = xmgd_scratch(3, (size_t)nctas * 2 *
-	    sizeof(double), &dpart)) != XMG_OK)
-		goto out;
-	st = launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
-	    (const task_meta *)(dbuf + tb), ntasks, nctas, (double *)dpart);
-	if (st != XMG_OK)
-		goto out;
+		return st;
+	XMG_CK(cudaMemcpyAsync((void *)dbuf, sorted.data(), (size_t)ntasks *
+	    sizeof(xmgd_ptask_t), cudaMemcpyHostToDevice, stream()));
+	XMG_CK(cudaMemcpyAsync((void *)(dbuf + tb), meta.data(), mb,
+	    cudaMemcpyHostToDevice, stream()));
+	if (dots && (st = xmgd_scratch(3, (size_t)nctas * 2 * sizeof(double),
+	    &dpart)) != XMG_OK)
+		return st;
+	if ((st = launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
+	    (const task_meta *)(dbuf + tb), ntasks, begin, (double *)dpart)))
+		return st;
 	/* the task buffers are reused by the next batch: wait here */
-	if ((st = check(cudaStreamSynchronize(stream()), "ptask_kernel")) !=
-	    XMG_OK)
-		goto out;
-	if (has_dot) {
-		double *h = (double *)malloc((size_t)nctas * 2 * sizeof(double));
-		if (h == NULL) {
-			st = xmg_seterr(XMG_ENOMEM, "out of memory");
-			goto out;
-		}
-		st = xmgd_d2h(h, dpart, (size_t)nctas * 2 * sizeof(double));
-		for (k = 0; st == XMG_OK && k < (size_t)ntasks; k++) {
-			int64_t e = k + 1 < (size_t)ntasks ? meta[k + 1].first_cta :
-			    nctas;
+	if ((st = check(cudaStreamSynchronize(stream()), "ptask_kernel")))
+		return st;
+	if (dots) {
+		std::vector<double> h((size_t)nctas * 2);
+		if ((st = xmgd_d2h(h.data(), dpart, h.size() * sizeof(double))))
+			return st;
+		for (int j = 0; j < ntasks; j++) {
+			const int64_t e = j + 1 < ntasks ? meta[j + 1].first_cta : nctas;
 			double a = 0, b = 0;
-			for (int64_t c = meta[k].first_cta; c < e; c++) {
+			for (int64_t c = meta[j].first_cta; c < e; c++) {
 				a += h[2 * c];
 				b += h[2 * c + 1];
 			}
-			dots[2 * k] = a;
-			dots[2 * k + 1] = b;
+			dots[2 * order[j]] = a;
+			dots[2 * order[j] + 1] = b;
 		}
-		free(h);
 	}
-out:
-	free(meta);
-	return st;
+	return XMG_OK;
 }

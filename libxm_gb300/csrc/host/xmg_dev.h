@@ -67,10 +67,14 @@ typedef struct {
 /* A batch uploaded once into a device buffer owned by the caller (release
  * with xmgd_free) and launched any number of times, also under stream
  * capture. */
-int xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, uint64_t *dbuf,
-    int64_t *nctas);
-int xmgd_ptask_launch(int dtype, int stype, uint64_t dbuf, int ntasks,
-    int64_t nctas);
+typedef struct {
+	uint64_t dbuf;               /* tasks + schedule metadata (xmgd_free) */
+	int ntasks;
+	int64_t begin[5];            /* CTA range of each schedule */
+} xmgd_ptask_batch_t;
+int xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, int stype,
+    xmgd_ptask_batch_t *b);
+int xmgd_ptask_launch(int dtype, int stype, const xmgd_ptask_batch_t *b);
 int xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
     double *dots);
 
