@@ -340,7 +340,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 	uint8_t *stages = reinterpret_cast<uint8_t *>(
 	    (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
 	__shared__ __align__(8) uint64_t bar_full[NST], bar_empty[NST];
-	__shared__ __align__(8) uint64_t bar_accfull, bar_xempty, bar_yempty, bar_fin;
+	__shared__ __align__(8) uint64_t bar_xfull, bar_yfull, bar_xempty, bar_yempty, bar_fin;
 	__shared__ __align__(8) uint64_t bar_ifull[2], bar_iempty[2];
 	__shared__ int s_item[2];
 	__shared__ uint32_t s_tmem;
@@ -358,7 +358,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			mbar_init(smem_u32(&bar_full[s]), 1);
 			mbar_init(smem_u32(&bar_empty[s]), 1);
 		}
-		mbar_init(smem_u32(&bar_accfull), 1);
+		mbar_init(smem_u32(&bar_xfull), 1);
+		mbar_init(smem_u32(&bar_yfull), 1);
 		mbar_init(smem_u32(&bar_xempty), DW);
 		mbar_init(smem_u32(&bar_yempty), DW);
 		mbar_init(smem_u32(&bar_fin), 1);
@@ -473,7 +474,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					const int nks = vb[pr.bview].n_ks;
 					for (int c0 = 0; c0 < nks && !s_err; ) {
 						const int c1 = chunk_end(c0, nks, cplx);
-						const int L = min(NST, c1 - c0);
+						/* head: the first H (staged) steps; tail: the last T
+						 * steps; middle: the rest */
+						const int H = min(NST, c1 - c0);
+						const int T = min(NST, c1 - c0 - H);
 						/* every accumulator restarts each chunk: the exact
 						 * groups for their 2^23 bound, the low band because
 						 * the tensor core's fp32 accumulation error grows
@@ -481,15 +485,15 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						 * accumulation measured 10x larger error) */
 						uint32_t started = 0;
 						bool okc = true;
-						/* set X of the first L (staged) K steps, as soon as
-						 * the drain has read X of the previous chunk */
+						/* head, set X, as soon as the drain has read X of
+						 * the previous chunk */
 						if (!first) {
 							if (!mbar_wait(smem_u32(&bar_xempty), xph, &s_err, g_err, 2))
 								break;
 							xph ^= 1;
 						}
 						tc_fence_after();
-						for (int j = 0; j < L; j++) {
+						for (int j = 0; j < H; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
 							const uint32_t pj = s + j < NST ? ph : ph ^ 1;
 							if (!mbar_wait(smem_u32(&bar_full[sj]), pj, &s_err, g_err, 3)) {
@@ -502,7 +506,9 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						}
 						if (!okc)
 							break;
-						/* set Y of the same steps once Y is read too */
+						if (T == 0)
+							mma_commit(smem_u32(&bar_xfull));
+						/* head, set Y, once Y is read too */
 						if (!first) {
 							if (!mbar_wait(smem_u32(&bar_yempty), yph, &s_err, g_err, 8))
 								break;
@@ -510,25 +516,56 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						}
 						first = false;
 						tc_fence_after();
-						for (int j = 0; j < L; j++) {
+						for (int j = 0; j < H; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
 							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
 							mma_commit(smem_u32(&bar_empty[sj]));
 						}
-						s += L;
+						s += H;
 						if (s >= NST) { s -= NST; ph ^= 1; }
-						/* the rest of the chunk: every product per step */
-						for (int ks = c0 + L; ks < c1; ks++) {
-							if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3))
+						/* middle: every product per step */
+						for (int ks = c0 + H; ks < c1 - T; ks++) {
+							if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3)) {
+								okc = false;
 								break;
+							}
 							tc_fence_after();
 							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)s *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 3, started);
 							mma_commit(smem_u32(&bar_empty[s]));
 							if (++s == NST) { s = 0; ph ^= 1; }
 						}
-						mma_commit(smem_u32(&bar_accfull));
+						if (!okc)
+							break;
+						/* tail: set X of the last T steps, then X is
+						 * complete and its drain can start while the
+						 * tensor core still works on set Y */
+						for (int j = 0; j < T; j++) {
+							const int sj = s + j < NST ? s + j : s + j - NST;
+							const uint32_t pj = s + j < NST ? ph : ph ^ 1;
+							if (!mbar_wait(smem_u32(&bar_full[sj]), pj, &s_err, g_err, 3)) {
+								okc = false;
+								break;
+							}
+							tc_fence_after();
+							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
+						}
+						if (!okc)
+							break;
+						if (T > 0) {
+							mma_commit(smem_u32(&bar_xfull));
+							for (int j = 0; j < T; j++) {
+								const int sj = s + j < NST ? s + j : s + j - NST;
+								issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+								    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
+								mma_commit(smem_u32(&bar_empty[sj]));
+							}
+							s += T;
+							if (s >= NST) { s -= NST; ph ^= 1; }
+						}
+						mma_commit(smem_u32(&bar_yfull));
 						c0 = c1;
 					}
 				}
@@ -588,13 +625,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					 * .sync.aligned TMEM loads below stay convergent */
 					int w = 1;
 					if (lane == 0)
-						w = mbar_wait(smem_u32(&bar_accfull), fph, &s_err, g_err, 4);
+						w = mbar_wait(smem_u32(&bar_xfull), fph, &s_err, g_err, 4);
 					w = __shfl_sync(0xffffffffu, w, 0);
 					if (!w) {
 						ok = false;
 						break;
 					}
-					fph ^= 1;
 					tc_fence_after();
 					/* set X first: the low band (or, without one, group 2),
 					 * then release it to the MMA warp */
@@ -627,7 +663,18 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					__syncwarp();
 					if (lane == 0)
 						mbar_arrive(smem_u32(&bar_xempty));
-					/* set Y: the exact groups below X */
+					/* set Y: the exact groups below X, once their last
+					 * products have landed */
+					w = 1;
+					if (lane == 0)
+						w = mbar_wait(smem_u32(&bar_yfull), fph, &s_err, g_err, 9);
+					w = __shfl_sync(0xffffffffu, w, 0);
+					if (!w) {
+						ok = false;
+						break;
+					}
+					fph ^= 1;
+					tc_fence_after();
 #pragma unroll
 					for (int b4 = 0; b4 < NC / 4; b4++) {
 						if (half * NC + b4 * 4 >= rows)
