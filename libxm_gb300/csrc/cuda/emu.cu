@@ -303,12 +303,17 @@ struct acc_sets {
 };
 
 /* the slice products of one K step whose accumulator lies in `which`
- * (1: set X, 2: set Y, 3: both) */
+ * (1: set X, 2: set Y, 3: both).  The two stage descriptors are built once;
+ * each product adds its slice offset (>> 4) to the low word, which cannot
+ * carry out of the 14-bit address field inside a < 256 KiB stage area. */
 template <int S, int KEEP>
 __device__ __forceinline__ void
 issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
     int which, uint32_t &started)
 {
+	const uint64_t da = sdesc(base, S * 256), db = sdesc(base + a_off, S * 256);
+	const uint32_t alo = (uint32_t)da, ahi = (uint32_t)(da >> 32);
+	const uint32_t blo = (uint32_t)db, bhi = (uint32_t)(db >> 32);
 #pragma unroll
 	for (int pa = 0; pa < S; pa++)
 #pragma unroll
@@ -318,9 +323,8 @@ issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
 			const int acc = min(pa + qb, 3);
 			if (!(which & (acc == acc_sets<KEEP>::XACC ? 1 : 2)))
 				continue;
-			uint64_t ad = sdesc(base + qb * 256, S * 256);
-			uint64_t bd = sdesc(base + a_off + pa * 256, S * 256);
-			mma_bf16(tmem + acc * 128, ad, bd, idesc, (started >> acc) & 1u);
+			mma_bf16_split(tmem + acc * 128, alo + qb * 16, ahi, blo + pa * 16,
+			    bhi, idesc, (started >> acc) & 1u);
 			started |= 1u << acc;
 		}
 }

@@ -123,6 +123,17 @@ __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b,
 	    :: "r"(d), "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
+/* the same with each descriptor passed as (low, high) words */
+__device__ __forceinline__ void mma_bf16_split(uint32_t d, uint32_t alo,
+    uint32_t ahi, uint32_t blo, uint32_t bhi, uint32_t idesc, uint32_t acc)
+{
+	asm volatile("{\n\t.reg .pred p;\n\t.reg .b64 a, b;\n\t"
+	    "mov.b64 a, {%1, %2};\n\tmov.b64 b, {%3, %4};\n\t"
+	    "setp.ne.b32 p, %6, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], a, b, %5, p;\n\t}"
+	    :: "r"(d), "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(acc));
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
 	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
