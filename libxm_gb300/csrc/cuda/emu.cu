@@ -124,8 +124,9 @@ template <typename T>
 __device__ __forceinline__ T fetch(const T *X, const int32_t *rowt, int32_t co,
     const xmgd_view_t &w, int k)
 {
-	if (!w.cplx)
+	if (!w.cplx) {
 		return k < w.k ? X[rowt[k] + co] : T(0);
+	}
 	const int half = k >= w.khp;
 	const int kk = k - half * w.khp;
 	return kk < w.k ? X[2 * (rowt[kk] + co) + half] : T(0);
@@ -306,7 +307,7 @@ struct acc_sets {
  * (1: set X, 2: set Y, 3: both).  The two stage descriptors are built once;
  * each product adds its slice offset (>> 4) to the low word, which cannot
  * carry out of the 14-bit address field inside a < 256 KiB stage area. */
-template <int S, int KEEP>
+template <int S, int KEEP, bool PAIR>
 __device__ __forceinline__ void
 issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
     int which, uint32_t &started)
@@ -323,13 +324,21 @@ issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
 			const int acc = min(pa + qb, 3);
 			if (!(which & (acc == acc_sets<KEEP>::XACC ? 1 : 2)))
 				continue;
-			mma_bf16_split(tmem + acc * 128, alo + qb * 16, ahi, blo + pa * 16,
-			    bhi, idesc, (started >> acc) & 1u);
+			if constexpr (PAIR)
+				mma_bf16_pair(tmem + acc * 128, alo + qb * 16, ahi, blo + pa * 16,
+				    bhi, idesc, (started >> acc) & 1u);
+			else
+				mma_bf16_split(tmem + acc * 128, alo + qb * 16, ahi, blo + pa * 16,
+				    bhi, idesc, (started >> acc) & 1u);
 			started |= 1u << acc;
 		}
 }
 
-template <int S, int KEEP, bool LOW, typename TOUT, int DW>
+/* PAIR: a cluster of two CTAs runs each 256-row tile with cta_group::2
+ * MMAs issued by rank 0: each CTA stages its own 128 M-side rows and half
+ * of the N side, rank 1 forwards its stage completions to rank 0, the
+ * drains of both CTAs read their own TMEM and release it to rank 0. */
+template <int S, int KEEP, bool LOW, typename TOUT, int DW, bool PAIR>
 __global__ void __launch_bounds__(64 + 32 * DW, 1)
 emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
     const xmgd_cblock_t *__restrict__ cbs, const xmgd_pair_t *__restrict__ prs,
@@ -346,6 +355,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 	__shared__ __align__(8) uint64_t bar_full[NST], bar_empty[NST];
 	__shared__ __align__(8) uint64_t bar_xfull, bar_yfull, bar_xempty, bar_yempty, bar_fin;
 	__shared__ __align__(8) uint64_t bar_ifull[2], bar_iempty[2];
+	__shared__ __align__(8) uint64_t bar_pfull[PAIR ? NST : 1];
 	__shared__ int s_item[2];
 	__shared__ uint32_t s_tmem;
 	__shared__ volatile int s_err;
@@ -356,6 +366,27 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 	if (*(volatile int *)flags & 1)
 		return;
 	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const uint32_t rank = PAIR ? cluster_rank() : 0;
+	/* bounded waits; in a pair, with cluster-scope acquire */
+	auto wait = [&](uint32_t bar, uint32_t parity, int code) -> bool {
+		if constexpr (PAIR)
+			return mbar_wait_cl(bar, parity, &s_err, g_err, code);
+		else
+			return mbar_wait(bar, parity, &s_err, g_err, code);
+	};
+	/* arrive on a barrier of rank 0 (locally there, remotely from rank 1) */
+	auto arrive0 = [&](uint64_t *bar) {
+		if (!PAIR || rank == 0)
+			mbar_arrive(smem_u32(bar));
+		else
+			mbar_arrive_remote(map_shared(smem_u32(bar), 0));
+	};
+	auto commit = [&](uint64_t *bar) {
+		if constexpr (PAIR)
+			mma_commit_pair(smem_u32(bar));
+		else
+			mma_commit(smem_u32(bar));
+	};
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < NST; s++) {
@@ -364,23 +395,36 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 		}
 		mbar_init(smem_u32(&bar_xfull), 1);
 		mbar_init(smem_u32(&bar_yfull), 1);
-		mbar_init(smem_u32(&bar_xempty), DW);
-		mbar_init(smem_u32(&bar_yempty), DW);
+		mbar_init(smem_u32(&bar_xempty), PAIR ? 2 * DW : DW);
+		mbar_init(smem_u32(&bar_yempty), PAIR ? 2 * DW : DW);
 		mbar_init(smem_u32(&bar_fin), 1);
 		for (int q = 0; q < 2; q++) {
 			mbar_init(smem_u32(&bar_ifull[q]), 1);
-			mbar_init(smem_u32(&bar_iempty[q]), 1 + DW);
+			/* pair: both CTAs' drains, rank 0's MMA warp, rank 1's
+			 * producer and forwarder */
+			mbar_init(smem_u32(&bar_iempty[q]), PAIR ? 2 * DW + 3 : 1 + DW);
 		}
+		if (PAIR)
+			for (int q = 0; q < NST; q++)
+				mbar_init(smem_u32(&bar_pfull[q]), 1);
 		s_err = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
 	if (warp == 1) {
-		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;"
-		    :: "r"(smem_u32(&s_tmem)));
-		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+		if constexpr (PAIR) {
+			asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], 512;"
+			    :: "r"(smem_u32(&s_tmem)));
+			asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+		} else {
+			asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;"
+			    :: "r"(smem_u32(&s_tmem)));
+			asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+		}
 	}
 	tc_fence_before();
 	__syncthreads();
+	if constexpr (PAIR)
+		cluster_sync();	/* peers' barriers exist before any remote arrive */
 	tc_fence_after();
 	const uint32_t tmem = s_tmem;
 
@@ -399,39 +443,61 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				lastp[q] = -1;
 			uint32_t iph = 0;
 			for (int slot = 0; !s_err; ) {
-				if (!mbar_wait(smem_u32(&bar_iempty[slot]), iph ^ 1, &s_err, g_err, 5))
-					break;
-				int t = atomicAdd(g_next, 1);
-				t = t < nitems ? t : -1;
-				s_item[slot] = t;
-				mbar_arrive(smem_u32(&bar_ifull[slot]));
+				int t;
+				if (!PAIR || rank == 0) {
+					/* fetch the next item and hand it to every role */
+					if (!wait(smem_u32(&bar_iempty[slot]), iph ^ 1, 5))
+						break;
+					t = atomicAdd(g_next, 1);
+					t = t < nitems ? t : -1;
+					s_item[slot] = t;
+					if (PAIR) {
+						st_remote_u32(map_shared(smem_u32(&s_item[slot]), 1), (uint32_t)t);
+						mbar_arrive_remote(map_shared(smem_u32(&bar_ifull[slot]), 1));
+					}
+					mbar_arrive(smem_u32(&bar_ifull[slot]));
+				} else {
+					if (!wait(smem_u32(&bar_ifull[slot]), iph, 5))
+						break;
+					t = s_item[slot];
+					arrive0(&bar_iempty[slot]);
+				}
 				if (++slot == 2) { slot = 0; iph ^= 1; }
 				if (t < 0)
 					break;
 				const emu_item it = items[t];
 				const xmgd_cblock_t cb = cbs[it.cblock];
 				const int pass = it.pr & 1, swp = (it.pr >> 1) & 1;
-				/* M side: 128 rows; N side: the live rows only */
-				const uint32_t nbytes = (uint32_t)(it.pr >> 8) * S * 32;
+				/* M side: 128 rows (this CTA's half of 256 in a pair);
+				 * N side: the live rows only (a pair: this CTA's half) */
+				const uint32_t nbytes = (uint32_t)(it.pr >> 8) * S * 32 / (PAIR ? 2 : 1);
+				const uint32_t noff = PAIR ? rank * nbytes : 0;
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
 					const xmgd_view_t wb = vb[pr.bview], wa = va[pr.aview];
 					const int nks = wb.n_ks, nh = nks / 2;
-					const uint8_t *gb = reinterpret_cast<const uint8_t *>(wb.slices) +
-					    (size_t)(it.j0 / EMU_TM) * nks * C::CHUNK_BYTES;
-					const uint8_t *ga = reinterpret_cast<const uint8_t *>(wa.slices) +
-					    (size_t)(it.i0 / EMU_TM) * nks * C::CHUNK_BYTES;
-					const uint8_t *gm = swp ? ga : gb, *gn = swp ? gb : ga;
+					const int mtile = (swp ? it.i0 : it.j0) / EMU_TM + (int)rank;
+					const int ntile = (swp ? it.j0 : it.i0) / EMU_TM;
+					const bool mlive = mtile < (swp ? wa.n_rt : wb.n_rt);
+					const uint8_t *gm = reinterpret_cast<const uint8_t *>(
+					    swp ? wa.slices : wb.slices) + (size_t)mtile * nks * C::CHUNK_BYTES;
+					const uint8_t *gn = reinterpret_cast<const uint8_t *>(
+					    swp ? wb.slices : wa.slices) + (size_t)ntile * nks * C::CHUNK_BYTES +
+					    noff;
 					for (int ks = 0; ks < nks; ks++) {
-						if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1, &s_err, g_err, 1))
+						if (!wait(smem_u32(&bar_empty[s]), ph ^ 1, 1))
 							break;
 						/* imaginary pass: B's re/im halves swapped */
 						const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
 						const int km = swp ? ks : kb, kn = swp ? kb : ks;
 						uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 						uint32_t fb = smem_u32(&bar_full[s]);
-						mbar_expect_tx(fb, C::CHUNK_BYTES + nbytes);
-						bulk_g2s(dst, gm + (size_t)km * C::CHUNK_BYTES, C::CHUNK_BYTES, fb);
+						/* a pair's second M tile may lie past the view: its
+						 * rows are then never stored */
+						mbar_expect_tx(fb, (mlive ? C::CHUNK_BYTES : 0) + nbytes);
+						if (mlive)
+							bulk_g2s(dst, gm + (size_t)km * C::CHUNK_BYTES,
+							    C::CHUNK_BYTES, fb);
 						bulk_g2s(dst + C::CHUNK_BYTES, gn + (size_t)kn * C::CHUNK_BYTES,
 						    nbytes, fb);
 #pragma unroll
@@ -455,6 +521,36 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 							;
 			}
 		}
+	} else if (warp == 1 && PAIR && rank == 1) {
+		/* ---------- rank 1: forward stage completions to rank 0 ---------- */
+		if (lane == 0) {
+			int s = 0;
+			uint32_t ph = 0, iph = 0;
+			for (int slot = 0; !s_err; ) {
+				if (!wait(smem_u32(&bar_ifull[slot]), iph, 6))
+					break;
+				const int t = s_item[slot];
+				arrive0(&bar_iempty[slot]);
+				if (++slot == 2) { slot = 0; iph ^= 1; }
+				if (t < 0)
+					break;
+				const xmgd_cblock_t cb = cbs[items[t].cblock];
+				for (int p = 0; p < cb.npairs && !s_err; p++) {
+					const int nks = vb[prs[cb.first_pair + p].bview].n_ks;
+					for (int ks = 0; ks < nks; ks++) {
+						if (!wait(smem_u32(&bar_full[s]), ph, 3))
+							break;
+						mbar_arrive_remote(map_shared(smem_u32(&bar_pfull[s]), 0));
+						if (++s == NST) { s = 0; ph ^= 1; }
+					}
+				}
+			}
+			/* rank 0's last MMAs (they write this CTA's TMEM) are done
+			 * once the final commit lands here */
+			uint64_t t0 = gtimer();
+			while (!mbar_try_cl(smem_u32(&bar_fin), 0) && gtimer() - t0 < WAIT_NS)
+				;
+		}
 	} else if (warp == 1) {
 		/* ---------------- MMA issuer ---------------- */
 		if (lane == 0) {
@@ -462,8 +558,17 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			bool first = true;
 			uint32_t ph = 0, xph = 0, yph = 0;
 			uint32_t iph = 0;
+			/* a stage is ready once this CTA's copies (and, in a pair,
+			 * the peer's, forwarded) have landed */
+			auto ready = [&](int st_, uint32_t par) -> bool {
+				if (!wait(smem_u32(&bar_full[st_]), par, 3))
+					return false;
+				if (PAIR && !wait(smem_u32(&bar_pfull[st_]), par, 10))
+					return false;
+				return true;
+			};
 			for (int slot = 0; !s_err; ) {
-				if (!mbar_wait(smem_u32(&bar_ifull[slot]), iph, &s_err, g_err, 6))
+				if (!wait(smem_u32(&bar_ifull[slot]), iph, 6))
 					break;
 				const int t = s_item[slot];
 				mbar_arrive(smem_u32(&bar_iempty[slot]));
@@ -472,7 +577,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					break;
 				const emu_item it = items[t];
 				const xmgd_cblock_t cb = cbs[it.cblock];
-				const uint32_t idesc = idesc_n(it.pr >> 8);
+				const uint32_t idesc = PAIR ? idesc_pair_n(it.pr >> 8) : idesc_n(it.pr >> 8);
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
 					const int nks = vb[pr.bview].n_ks;
@@ -492,7 +597,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						/* head, set X, as soon as the drain has read X of
 						 * the previous chunk */
 						if (!first) {
-							if (!mbar_wait(smem_u32(&bar_xempty), xph, &s_err, g_err, 2))
+							if (!wait(smem_u32(&bar_xempty), xph, 2))
 								break;
 							xph ^= 1;
 						}
@@ -500,21 +605,21 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						for (int j = 0; j < H; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
 							const uint32_t pj = s + j < NST ? ph : ph ^ 1;
-							if (!mbar_wait(smem_u32(&bar_full[sj]), pj, &s_err, g_err, 3)) {
+							if (!ready(sj, pj)) {
 								okc = false;
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
 						}
 						if (!okc)
 							break;
 						if (T == 0)
-							mma_commit(smem_u32(&bar_xfull));
+							commit(&bar_xfull);
 						/* head, set Y, once Y is read too */
 						if (!first) {
-							if (!mbar_wait(smem_u32(&bar_yempty), yph, &s_err, g_err, 8))
+							if (!wait(smem_u32(&bar_yempty), yph, 8))
 								break;
 							yph ^= 1;
 						}
@@ -522,22 +627,22 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						tc_fence_after();
 						for (int j = 0; j < H; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
-							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
-							mma_commit(smem_u32(&bar_empty[sj]));
+							commit(&bar_empty[sj]);
 						}
 						s += H;
 						if (s >= NST) { s -= NST; ph ^= 1; }
 						/* middle: every product per step */
 						for (int ks = c0 + H; ks < c1 - T; ks++) {
-							if (!mbar_wait(smem_u32(&bar_full[s]), ph, &s_err, g_err, 3)) {
+							if (!ready(s, ph)) {
 								okc = false;
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)s *
+							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)s *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 3, started);
-							mma_commit(smem_u32(&bar_empty[s]));
+							commit(&bar_empty[s]);
 							if (++s == NST) { s = 0; ph ^= 1; }
 						}
 						if (!okc)
@@ -548,37 +653,38 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						for (int j = 0; j < T; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
 							const uint32_t pj = s + j < NST ? ph : ph ^ 1;
-							if (!mbar_wait(smem_u32(&bar_full[sj]), pj, &s_err, g_err, 3)) {
+							if (!ready(sj, pj)) {
 								okc = false;
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
 							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
 						}
 						if (!okc)
 							break;
 						if (T > 0) {
-							mma_commit(smem_u32(&bar_xfull));
+							commit(&bar_xfull);
 							for (int j = 0; j < T; j++) {
 								const int sj = s + j < NST ? s + j : s + j - NST;
-								issue_step<S, KEEP>(tmem, smem_u32(stages + (size_t)sj *
+								issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
 								    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
-								mma_commit(smem_u32(&bar_empty[sj]));
+								commit(&bar_empty[sj]);
 							}
 							s += T;
 							if (s >= NST) { s -= NST; ph ^= 1; }
 						}
-						mma_commit(smem_u32(&bar_yfull));
+						commit(&bar_yfull);
 						c0 = c1;
 					}
 				}
 			}
 			/* every MMA issued by this CTA has completed once bar_fin
 			 * fires; TMEM is released only after that */
-			mma_commit(smem_u32(&bar_fin));
+			commit(&bar_fin);
 			uint64_t t0 = gtimer();
-			while (!mbar_try(smem_u32(&bar_fin), 0) && gtimer() - t0 < WAIT_NS)
+			while (!(PAIR ? mbar_try_cl(smem_u32(&bar_fin), 0) :
+			    mbar_try(smem_u32(&bar_fin), 0)) && gtimer() - t0 < WAIT_NS)
 				;
 		}
 	} else {
@@ -594,9 +700,9 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 		for (int slot = 0; ok; ) {
 			int t = -1;
 			if (lane == 0) {
-				if (mbar_wait(smem_u32(&bar_ifull[slot]), iph, &s_err, g_err, 7)) {
+				if (wait(smem_u32(&bar_ifull[slot]), iph, 7)) {
 					t = s_item[slot];
-					mbar_arrive(smem_u32(&bar_iempty[slot]));
+					arrive0(&bar_iempty[slot]);
 				} else
 					t = -2;
 			}
@@ -629,7 +735,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					 * .sync.aligned TMEM loads below stay convergent */
 					int w = 1;
 					if (lane == 0)
-						w = mbar_wait(smem_u32(&bar_xfull), fph, &s_err, g_err, 4);
+						w = wait(smem_u32(&bar_xfull), fph, 4);
 					w = __shfl_sync(0xffffffffu, w, 0);
 					if (!w) {
 						ok = false;
@@ -666,12 +772,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					tc_fence_before();
 					__syncwarp();
 					if (lane == 0)
-						mbar_arrive(smem_u32(&bar_xempty));
+						arrive0(&bar_xempty);
 					/* set Y: the exact groups below X, once their last
 					 * products have landed */
 					w = 1;
 					if (lane == 0)
-						w = mbar_wait(smem_u32(&bar_yfull), fph, &s_err, g_err, 9);
+						w = wait(smem_u32(&bar_yfull), fph, 9);
 					w = __shfl_sync(0xffffffffu, w, 0);
 					if (!w) {
 						ok = false;
@@ -704,7 +810,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					tc_fence_before();
 					__syncwarp();
 					if (lane == 0)
-						mbar_arrive(smem_u32(&bar_yempty));
+						arrive0(&bar_yempty);
 					c0 = c1;
 				}
 			}
@@ -714,7 +820,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			 * this thread's TMEM lane is one M-side row; its columns are
 			 * N-side rows.  Without swap the M side is b's free index (j),
 			 * with swap a's (i). */
-			const int ms = (swp ? it.i0 : it.j0) + quad * 32 + lane;
+			const int ms = (swp ? it.i0 : it.j0) + (int)rank * EMU_TM + quad * 32 + lane;
 			const int q0 = (swp ? it.j0 : it.i0) + half * NC;
 			const int flim = swp ? cb.m : cb.n, vlim = swp ? cb.n : cb.m;
 			if (ms < flim) {
@@ -741,9 +847,18 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
-	if (warp == 1)
-		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;"
-		    :: "r"(tmem));
+	if (warp == 1) {
+		if constexpr (PAIR)
+			asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, 512;"
+			    :: "r"(tmem));
+		else
+			asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;"
+			    :: "r"(tmem));
+	}
+	/* neither CTA of a pair leaves while the other may still arrive on
+	 * its barriers */
+	if constexpr (PAIR)
+		cluster_sync();
 }
 
 /* ------------------------------------------------------------------ */
@@ -766,11 +881,20 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
  */
 enum { EMU_NPOLICY = 3 };
 
+/* CTA pairs (256-row M tiles, cta_group::2): policies 3..5 repeat 0..2 in
+ * that form; offered to the tuner when XMG_CTA_PAIR=1 */
+static bool
+pairs_enabled()
+{
+	const char *e = getenv("XMG_CTA_PAIR");
+	return e && strcmp(e, "1") == 0;
+}
+
 static double
-tile_cost(int mside, int nside, int policy)
+tile_cost(int mside, int nside, int policy, int mrows)
 {
 	double c = 0;
-	const int mt = (mside + EMU_TM - 1) / EMU_TM;
+	const int mt = (mside + mrows - 1) / mrows;
 	for (int n0 = 0; n0 < nside; n0 += EMU_TM) {
 		const int w = std::min(EMU_TM, (nside - n0 + 15) / 16 * 16);
 		c += policy == 2 ? std::max(w / 2.0, 32.0 + w / 4.0) : (double)w;
@@ -868,12 +992,33 @@ launch_gemm(emu_plan *e)
 	int32_t *EA = (int32_t *)e->d_E, *EB = EA + e->nexp_a;
 	int *flags = (int *)(EA + e->nE);
 
-	emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW><<<(unsigned)c.grid,
-	    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
-	    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
-	    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
-	    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
-	    2 * fin<TIN>::EXPOFF, e->cplx, flags);
+	if (c.policy >= EMU_NPOLICY) {
+		/* clusters of two CTAs */
+		cudaLaunchConfig_t cfg = {};
+		cudaLaunchAttribute at[1];
+		at[0].id = cudaLaunchAttributeClusterDimension;
+		at[0].val.clusterDim.x = 2;
+		at[0].val.clusterDim.y = 1;
+		at[0].val.clusterDim.z = 1;
+		cfg.gridDim = dim3((unsigned)c.grid);
+		cfg.blockDim = dim3(64 + 32 * EMU_DW);
+		cfg.dynamicSmemBytes = stage_cfg<S>::SMEM;
+		cfg.stream = stream();
+		cfg.attrs = at;
+		cfg.numAttrs = 1;
+		XMG_CK(cudaLaunchKernelEx(&cfg, emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, true>,
+		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
+		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
+		    (const int32_t *)EA, (const int32_t *)EB, (const int32_t *)e->d_F,
+		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, flags));
+	} else {
+		emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, false><<<(unsigned)c.grid,
+		    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
+		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
+		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
+		    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
+		    2 * fin<TIN>::EXPOFF, e->cplx, flags);
+	}
 	g_launches++;
 	XMG_CK(cudaGetLastError());
 	XMG_CK(cudaMemcpyAsync(e->h_flags, flags, 2 * sizeof(int),
@@ -888,7 +1033,9 @@ set_attrs()
 	constexpr int S = fin<TIN>::S, KEEP = fin<TIN>::KEEP;
 	static bool done = false;
 	if (!done) {
-		XMG_CK(cudaFuncSetAttribute(emu_gemm_kernel<S, KEEP, (KEEP > 2), TOUT, EMU_DW>,
+		XMG_CK(cudaFuncSetAttribute(emu_gemm_kernel<S, KEEP, (KEEP > 2), TOUT, EMU_DW, false>,
+		    cudaFuncAttributeMaxDynamicSharedMemorySize, stage_cfg<S>::SMEM));
+		XMG_CK(cudaFuncSetAttribute(emu_gemm_kernel<S, KEEP, (KEEP > 2), TOUT, EMU_DW, true>,
 		    cudaFuncAttributeMaxDynamicSharedMemorySize, stage_cfg<S>::SMEM));
 		done = true;
 	}
@@ -943,13 +1090,15 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 	items.clear();
 	for (auto &o : order) {
 		const xmgd_cblock_t &cb = p->cblocks[o.second];
+		const int orient = policy % EMU_NPOLICY;
+		const int mstep = policy >= EMU_NPOLICY ? 2 * EMU_TM : EMU_TM;
 		bool swp = false;
-		if (policy != 1) {
-			const int pol = policy == 2 ? 2 : 0;
-			swp = tile_cost(cb.m, cb.n, pol) < tile_cost(cb.n, cb.m, pol);
+		if (orient != 1) {
+			const int pol = orient == 2 ? 2 : 0;
+			swp = tile_cost(cb.m, cb.n, pol, mstep) < tile_cost(cb.n, cb.m, pol, mstep);
 		}
 		const int mlen = swp ? cb.m : cb.n, nlen = swp ? cb.n : cb.m;
-		for (int m0 = 0; m0 < mlen; m0 += EMU_TM)
+		for (int m0 = 0; m0 < mlen; m0 += mstep)
 			for (int n0 = 0; n0 < nlen; n0 += EMU_TM) {
 				const int rows = std::min(EMU_TM, (nlen - n0 + 15) / 16 * 16);
 				const int i0 = swp ? m0 : n0, j0 = swp ? n0 : m0;
@@ -1089,8 +1238,10 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 			known = t.policy;
 	if (getenv("XMG_TUNE") && strcmp(getenv("XMG_TUNE"), "0") == 0)
 		known = 0;
+	if (getenv("XMG_POLICY"))	/* one fixed work-list policy */
+		known = atoi(getenv("XMG_POLICY"));
 	std::vector<std::vector<emu_item>> lists;
-	for (int pol = 0; pol < EMU_NPOLICY; pol++) {
+	for (int pol = 0; pol < (pairs_enabled() ? 2 : 1) * EMU_NPOLICY; pol++) {
 		if (known >= 0 && pol != known)
 			continue;
 		std::vector<emu_item> items;
@@ -1104,7 +1255,8 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		emu_cand c;
 		c.policy = pol;
 		c.nitems = (int)items.size();
-		c.grid = std::min(c.nitems, num_sms());
+		c.grid = pol >= EMU_NPOLICY ? 2 * std::min(c.nitems, num_sms() / 2) :
+		    std::min(c.nitems, num_sms());
 		c.ms = -1;
 		if ((st = upload_new(items.data(), items.size() * sizeof(emu_item),
 		    &c.d_items)))

@@ -23,6 +23,13 @@ __host__ __device__ constexpr uint32_t idesc_n(int n)
 	return IDESC_M128 | ((uint32_t)(n >> 3) << 17);
 }
 
+/* M = 256 over a CTA pair */
+__host__ __device__ constexpr uint32_t idesc_pair_n(int n)
+{
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 4) << 24) |
+	    ((uint32_t)(n >> 3) << 17);
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
 	return (uint32_t)__cvta_generic_to_shared(p);
@@ -181,6 +188,95 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 __device__ __forceinline__ void tmem_wait_ld()
 {
 	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+/* ---- CTA pairs (cluster of two, cta_group::2) ----------------------- */
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+	uint32_t r;
+	asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+	return r;
+}
+
+/* the shared::cluster address of `addr` (a shared::cta address of this
+ * CTA's layout) in the CTA of cluster rank `rank` */
+__device__ __forceinline__ uint32_t map_shared(uint32_t addr, uint32_t rank)
+{
+	uint32_t r;
+	asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+	return r;
+}
+
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr)
+{
+	asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];"
+	    :: "r"(cluster_addr) : "memory");
+}
+
+__device__ __forceinline__ void st_remote_u32(uint32_t cluster_addr, uint32_t v)
+{
+	asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(cluster_addr), "r"(v) : "memory");
+}
+
+/* try-wait with cluster-scope acquire: for barriers that peers arrive on */
+__device__ __forceinline__ bool mbar_try_cl(uint32_t bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+	    "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+	return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cl(uint32_t bar, uint32_t parity,
+    volatile int *s_err, int *g_err, int code)
+{
+	if (mbar_try_cl(bar, parity))
+		return true;
+	uint64_t t0 = gtimer();
+	for (uint32_t n = 1;; n++) {
+		if (mbar_try_cl(bar, parity))
+			return true;
+		if ((n & 15) == 0) {
+			if (*s_err)
+				return false;
+			if (gtimer() - t0 > WAIT_NS) {
+				*s_err = code;
+				atomicMax(g_err, code);
+				return false;
+			}
+		}
+	}
+}
+
+/* all threads of both CTAs */
+__device__ __forceinline__ void cluster_sync()
+{
+	asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+	    "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+/* tensor-core MMA over the CTA pair: M = 256 (128 rows from each CTA's
+ * shared memory at the same offset), the N side split between the CTAs'
+ * shared memory, each CTA's TMEM receiving its 128 rows */
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d, uint32_t alo,
+    uint32_t ahi, uint32_t blo, uint32_t bhi, uint32_t idesc, uint32_t acc)
+{
+	asm volatile("{\n\t.reg .pred p;\n\t.reg .b64 a, b;\n\t"
+	    "mov.b64 a, {%1, %2};\n\tmov.b64 b, {%3, %4};\n\t"
+	    "setp.ne.b32 p, %6, 0;\n\t"
+	    "tcgen05.mma.cta_group::2.kind::f16 [%0], a, b, %5, p;\n\t}"
+	    :: "r"(d), "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(acc));
+}
+
+/* arrive on the barrier at this offset in both CTAs once every earlier
+ * pair MMA of this thread has completed */
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar)
+{
+	asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster"
+	    ".multicast::cluster.b64 [%0], %1;" :: "r"(bar), "h"((uint16_t)3) : "memory");
 }
 
 

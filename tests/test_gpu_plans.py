@@ -136,3 +136,24 @@ def test_inf_operand_in_replayed_plan(engine, oracle, gal, oal):
         engine.check(engine.xmg_set_precision(api.PREC_AUTO))
         w.free()
         wo.free()
+
+
+def test_cta_pair_kernel(engine, oracle, gal, oal, monkeypatch):
+    """The opt-in CTA-pair form of the split-precision GEMM (256-row tiles,
+    cta_group::2 MMAs over a cluster of two CTAs) gives the oracle's result.
+    The work-list policy is fixed to the pair form through the environment
+    (read when a plan is built)."""
+    monkeypatch.setenv("XMG_CTA_PAIR", "1")
+    monkeypatch.setenv("XMG_POLICY", "3")
+    w, wo = _pair(engine, oracle, gal, oal, seed=9)
+    try:
+        engine.check(engine.xmg_set_precision(api.PREC_EMU64))
+        wo.run()
+        for _ in range(2):
+            w.run()
+            assert api.last_stats(engine).precision_used == api.PREC_EMU64
+            assert _rel(w, wo) <= REL
+    finally:
+        engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+        w.free()
+        wo.free()
