@@ -865,16 +865,20 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 /* host side: a reusable plan with an online tile-orientation autotuner  */
 
 /*
- * Tile orientation per output block.  The M side of a tile is always 128
- * rows (TMEM lanes); the N side is the live rows rounded up to 16, so the
- * choice of which operand lies on the N side sets the padded work.  Three
- * policies, each a complete work list:
- *   0  per block, the orientation with less padded MMA work;
- *   1  a on the N side everywhere;
- *   2  per block, the cheaper orientation under a shared-memory model of
- *      one K step, max(N / 2, 32 + N / 4) cycles: the M-side operand
- *      (4 KiB) and the N-side operand (N * 32 B) are read from shared
- *      memory at 128 B per cycle while the tensor core needs N / 2 cycles.
+ * Work-list policies.  The M side of a tile is always 128 rows (TMEM
+ * lanes); the N side is the live rows rounded up to 16, so which operand
+ * lies on the N side sets the padded work, and the order of the items
+ * sets which tiles run together (L2 reuse: output blocks with the same
+ * M-side free block read the same M-side operand rows).  Three policies,
+ * each a complete work list:
+ *   0  per block the orientation with less padded MMA work; blocks by
+ *      decreasing cost, each block's tiles together;
+ *   1  the same orientation; blocks grouped by their M-side free block and
+ *      the group run M tile by M tile across its blocks;
+ *   2  grouped as 1, orientation from a shared-memory model of one K step,
+ *      max(N / 2, 32 + N / 4) cycles: the M-side operand (4 KiB) and the
+ *      N-side operand (N * 32 B) are read from shared memory at 128 B per
+ *      cycle while the tensor core needs N / 2 cycles.
  * The first runs of a plan replay each distinct policy once, timed with
  * events, then keep the fastest; the choice is remembered per block-size
  * histogram so later plans of the same shape start tuned.
@@ -1073,39 +1077,81 @@ emu_free(emu_plan *e)
 	delete e;
 }
 
-/* work list of one policy: blocks by decreasing cost, tiles adjacent */
+/* work list of one policy (see above) */
 static void
 make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
     int policy, std::vector<emu_item> &items)
 {
-	std::vector<std::pair<double, int>> order;
+	struct blk {
+		int ci, swp, mlen, nlen;
+		double cost;
+		uint64_t key;
+	};
+	const int base = policy % EMU_NPOLICY;
+	const int mstep = policy >= EMU_NPOLICY ? 2 * EMU_TM : EMU_TM;
+	const int pol = base == 2 ? 2 : 0;
+	std::vector<blk> bl;
 	for (int ci : cblocks) {
 		const xmgd_cblock_t &cb = p->cblocks[ci];
-		double c = 0;
+		double k = 0;
 		for (int q = 0; q < cb.npairs; q++)
-			c += p->pairs[cb.first_pair + q].k;
-		order.push_back({-c * cb.m * (double)cb.n, ci});
+			k += p->pairs[cb.first_pair + q].k;
+		blk b;
+		b.ci = ci;
+		b.swp = tile_cost(cb.m, cb.n, pol, mstep) < tile_cost(cb.n, cb.m, pol, mstep);
+		b.mlen = b.swp ? cb.m : cb.n;
+		b.nlen = b.swp ? cb.n : cb.m;
+		b.cost = k * cb.m * (double)cb.n;
+		/* the M-side free block (its exponent-table slot names it) */
+		b.key = ((uint64_t)b.swp << 40) | (uint32_t)(b.swp ? cb.eA : cb.eB);
+		bl.push_back(b);
 	}
-	std::stable_sort(order.begin(), order.end());
-	items.clear();
-	for (auto &o : order) {
-		const xmgd_cblock_t &cb = p->cblocks[o.second];
-		const int orient = policy % EMU_NPOLICY;
-		const int mstep = policy >= EMU_NPOLICY ? 2 * EMU_TM : EMU_TM;
-		bool swp = false;
-		if (orient != 1) {
-			const int pol = orient == 2 ? 2 : 0;
-			swp = tile_cost(cb.m, cb.n, pol, mstep) < tile_cost(cb.n, cb.m, pol, mstep);
+	auto emit = [&](const blk &b, int m0) {
+		for (int n0 = 0; n0 < b.nlen; n0 += EMU_TM) {
+			const int rows = std::min(EMU_TM, (b.nlen - n0 + 15) / 16 * 16);
+			const int i0 = b.swp ? m0 : n0, j0 = b.swp ? n0 : m0;
+			for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
+				items.push_back(emu_item{b.ci, j0, i0,
+				    ps | (b.swp ? 2 : 0) | (rows << 8)});
 		}
-		const int mlen = swp ? cb.m : cb.n, nlen = swp ? cb.n : cb.m;
-		for (int m0 = 0; m0 < mlen; m0 += mstep)
-			for (int n0 = 0; n0 < nlen; n0 += EMU_TM) {
-				const int rows = std::min(EMU_TM, (nlen - n0 + 15) / 16 * 16);
-				const int i0 = swp ? m0 : n0, j0 = swp ? n0 : m0;
-				for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
-					items.push_back(emu_item{o.second, j0, i0,
-					    ps | (swp ? 2 : 0) | (rows << 8)});
-			}
+	};
+	items.clear();
+	std::stable_sort(bl.begin(), bl.end(),
+	    [](const blk &x, const blk &y) { return x.cost > y.cost; });
+	if (base == 0) {
+		for (const blk &b : bl)
+			for (int m0 = 0; m0 < b.mlen; m0 += mstep)
+				emit(b, m0);
+		return;
+	}
+	/* grouped: blocks reading the same M-side rows together, M tile by
+	 * M tile, groups by decreasing cost */
+	std::vector<std::pair<uint64_t, std::vector<int>>> groups;
+	std::vector<double> gcost;
+	for (int i = 0; i < (int)bl.size(); i++) {
+		size_t g = 0;
+		while (g < groups.size() && groups[g].first != bl[i].key)
+			g++;
+		if (g == groups.size()) {
+			groups.push_back({bl[i].key, {}});
+			gcost.push_back(0);
+		}
+		groups[g].second.push_back(i);
+		gcost[g] += bl[i].cost;
+	}
+	std::vector<int> go(groups.size());
+	for (size_t g = 0; g < go.size(); g++)
+		go[g] = (int)g;
+	std::stable_sort(go.begin(), go.end(),
+	    [&](int x, int y) { return gcost[x] > gcost[y]; });
+	for (int g : go) {
+		int mmax = 0;
+		for (int i : groups[g].second)
+			mmax = std::max(mmax, bl[i].mlen);
+		for (int m0 = 0; m0 < mmax; m0 += mstep)
+			for (int i : groups[g].second)
+				if (m0 < bl[i].mlen)
+					emit(bl[i], m0);
 	}
 }
 
