@@ -227,7 +227,7 @@ def block_costs(w):
 
 # DRAM bytes (read + write) of one split-precision GEMM launch on the cfg2
 # ladder, from a single-pass ncu capture of that kernel on this workload
-GEMM_DRAM_BYTES = 127.71e9 + 0.74062e9
+GEMM_DRAM_BYTES = 141.50e9 + 0.73965e9
 
 
 def make_workload(lib, al, scale=1, subset=None):
