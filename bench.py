@@ -49,6 +49,8 @@ def parse():
                    help="skip the pagefile-streamed measurement")
     p.add_argument("--no-elementwise", action="store_true",
                    help="skip the xm_set / xm_add bandwidth measurement")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the other measured configurations (cfg1, cfg3, cfg4)")
     p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
     p.add_argument("--subset", type=str, default=None,
                    help="O,V: keep the first O occupied and V virtual blocks (profiling case)")
@@ -230,6 +232,83 @@ def block_costs(w):
 GEMM_DRAM_BYTES = 141.50e9 + 0.73965e9
 
 
+def timed_calls(eng, fn, reps=3):
+    """Device time per call of fn after one untimed call (plan, tuning)."""
+    fn()
+    fn()
+    fn()
+    eng.check(eng.xmg_synchronize())
+    eng.check(eng.xmg_timer_start())
+    for _ in range(reps):
+        fn()
+    return eng.xmg_timer_stop() / reps
+
+
+def other_configs(eng, api, W):
+    """The remaining measured configurations at full size: the plain FP64
+    ladder cfg1, the permuted ring term cfg3 in float32 and complex128
+    (o = 64 as 4 x 16, v = 256 as 8 x 32, beta = 1, C prefilled), and the
+    adjoint of the cfg2 ladder (cfg4: dA and dB in one call).  Accuracy of
+    the float32 ring term: against the same contraction in FP64 on the GPU
+    (plain path) over identical, float-rounded inputs."""
+    out = {}
+    al = api.Allocator(eng)
+    eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+    # cfg1
+    w = W.cfg1(eng, al)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+    ms = timed_calls(eng, w.run)
+    out["cfg1_ladder_o24_v64"] = {"ms": ms, "tflops": fl / ms / 1e9, "useful_flops": fl,
+                                  "precision_used": api.last_stats(eng).precision_used}
+    w.free()
+    # cfg3 float32, with an FP64 twin for the error
+    w = W.cfg3(eng, al, dtype=api.FLOAT)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+    c0 = W.read_canonical(w.c)
+    wd = W.cfg3(eng, al, dtype=api.DOUBLE)
+    for ts, td in zip(w.tensors(), wd.tensors()):
+        for blk in ts.canonical_blocks():
+            td.write_block(blk, ts.read_block(blk).astype(np.float64))
+    ms = timed_calls(eng, w.run)
+    used = api.last_stats(eng).precision_used
+    for blk, x in c0.items():           # restore C, then one more call: beta = 1
+        w.c.write_block(blk, x)
+    w.run()
+    eng.check(eng.xmg_set_precision(api.PREC_FP64))
+    wd.run()
+    eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+    rel = W.rel_frobenius(W.read_canonical(w.c), W.read_canonical(wd.c))
+    out["cfg3_ring_o64_v256_f32"] = {"ms": ms, "tflops": fl / ms / 1e9, "useful_flops": fl,
+                                     "precision_used": used, "rel_err_vs_fp64": rel}
+    w.free()
+    wd.free()
+    # cfg3 complex128
+    w = W.cfg3(eng, al, dtype=api.DOUBLE_COMPLEX)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+    ms = timed_calls(eng, w.run)
+    out["cfg3_ring_o64_v256_c128"] = {"ms": ms, "tflops": fl / ms / 1e9, "useful_flops": fl,
+                                      "precision_used": api.last_stats(eng).precision_used}
+    w.free()
+    # cfg4: the adjoint of the cfg2 ladder, dA and dB
+    w = W.cfg2(eng, al)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+    dc = w.c.structure()
+    W.fill(dc, 77, W.LADDER_ANTISYM)
+    da, db = w.a.structure(), w.b.structure()
+
+    def adj():
+        eng.check(eng.xm_contract_adjoint(api.Scalar.of(1.0), w.a.h, w.b.h, dc.h, da.h, db.h,
+                                          b"ijcd", b"cdab", b"ijab"))
+    ms = timed_calls(eng, adj)
+    out["cfg4_adjoint_cfg2"] = {"ms": ms, "tflops": 2 * fl / ms / 1e9, "useful_flops": 2 * fl,
+                                "note": "dA and dB: two contractions of the cfg2 size plus the folds"}
+    for x in (dc, da, db):
+        x.free()
+    w.free()
+    al.destroy()
+    return out
+
+
 def make_workload(lib, al, scale=1, subset=None):
     from libxm_gb300 import workloads as W
     ob, vb = (int(x) for x in subset.split(",")) if subset else (None, None)
@@ -368,6 +447,8 @@ def engine_arm(args, ranks):
         pal.destroy()
         os.rmdir(tmp)
 
+    configs = None if args.no_configs or ranks.rank != 0 else other_configs(eng, api, W)
+
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
 
@@ -443,7 +524,7 @@ def engine_arm(args, ranks):
         "precision_used": "emu64" if emu["precision_used"] == api.PREC_EMU64 else "fp64",
         "phases_ms": {"gemm": emu["gemm_ms"], "split": emu["split_ms"]},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "out_of_core": ooc,
-        "elementwise": elem,
+        "elementwise": elem, "other_configs": configs,
         "gpu_launches": emu["launches"], "clocks": emu["clocks"],
         "setup_s": setup_s,
     }
