@@ -36,6 +36,29 @@ def test_exports_every_declared_symbol(engine):
     assert missing == []
 
 
+@pytest.mark.parametrize("prog", ["test.c", "example.c"])
+def test_reference_programs_link_unchanged(engine, prog):
+    """The reference's own test driver and example program compile against
+    include/ and link against the engine library, unchanged (they run only
+    where a GPU is present, and their sources only where the reference
+    checkout is)."""
+    import shutil
+    import subprocess
+    import oracle.build as ob
+    src = os.path.join(os.path.dirname(ob.REF_SRC), prog)
+    if not os.path.exists(src) or shutil.which("gcc") is None:
+        pytest.skip("reference sources or gcc not present")
+    libdir = os.path.join(ROOT, "libxm_gb300", "lib")
+    with tempfile.TemporaryDirectory() as d:
+        obj, exe = os.path.join(d, "p.o"), os.path.join(d, "p")
+        r = subprocess.run(["gcc", "-std=gnu99", "-I", os.path.join(ROOT, "include"), "-c",
+                            src, "-o", obj], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run(["gcc", "-o", exe, obj, "-L", libdir, "-lxmgb",
+                            "-Wl,-rpath," + libdir, "-lm"], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
 def test_exports_reference_test_driver_privates(engine):
     # test.c calls xm_fatal and xm_make_masks (util.h:34-35)
     assert hasattr(engine.dll, "xm_fatal") and hasattr(engine.dll, "xm_make_masks")
