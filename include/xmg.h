@@ -138,6 +138,13 @@ int xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b,
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
 
+/* Failure-detection self-test (no counterpart in the reference): one
+ * thread block waits on a barrier that nothing arrives at, through the
+ * bounded-wait path of the GEMM pipelines, gives up after timeout_us and
+ * returns; the expected result is XMG_ETIMEOUT with the device still
+ * usable.  Nothing faults or hangs. */
+int xmg_selftest_bounded_wait(unsigned timeout_us);
+
 /* xmg_contract keeps a device plan (metadata, work lists and a CUDA graph
  * of the launch sequence) for its most recent contractions over GPU-
  * resident tensors and replays it while the tensors' block tables are

@@ -68,9 +68,10 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 	return ok != 0;
 }
 
-/* Bounded wait; false on timeout or when another role already failed. */
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
-    volatile int *s_err, int *g_err, int code)
+/* Bounded wait; false on timeout (after limit_ns, recording `code` in the
+ * CTA's and the launch's error flags) or when another role already failed. */
+__device__ __forceinline__ bool mbar_wait_for(uint32_t bar, uint32_t parity,
+    volatile int *s_err, int *g_err, int code, uint64_t limit_ns)
 {
 	if (mbar_try(bar, parity))
 		return true;
@@ -84,13 +85,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
 		if ((n & 15) == 0) {
 			if (*s_err)
 				return false;
-			if (gtimer() - t0 > WAIT_NS) {
+			if (gtimer() - t0 > limit_ns) {
 				*s_err = code;
 				atomicMax(g_err, code);
 				return false;
 			}
 		}
 	}
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+    volatile int *s_err, int *g_err, int code)
+{
+	return mbar_wait_for(bar, parity, s_err, g_err, code, WAIT_NS);
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src,
