@@ -138,6 +138,15 @@ int xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b,
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
 
+/* Opt-in tile-aware autosplit (no counterpart in the reference, whose
+ * xm_block_space_autosplit is unchanged): every dimension is cut into about
+ * dim / target parts, each a whole multiple of quantum (the last one also
+ * takes the remainder below a quantum), so that the contraction's tiles
+ * (N widths in multiples of 16, 128-row M tiles) carry less padding.
+ * The block space must not be split yet. */
+int xmg_block_space_autosplit_tiles(xm_block_space_t *bs, size_t target,
+    size_t quantum);
+
 /* Failure-detection self-test (no counterpart in the reference): one
  * thread block waits on a barrier that nothing arrives at, through the
  * bounded-wait path of the GEMM pipelines, gives up after timeout_us and

@@ -128,6 +128,7 @@ _GB_SIGS = {
     "xmg_plan_cache_clear": (None, []),
     "xmg_set_staging": (C.c_int, [C.c_size_t, C.c_size_t]),
     "xmg_selftest_bounded_wait": (C.c_int, [C.c_uint]),
+    "xmg_block_space_autosplit_tiles": (C.c_int, [_P, C.c_size_t, C.c_size_t]),
     "xm_contract_adjoint": (C.c_int, [Scalar, _P, _P, _P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p]),
     "xmg_timer_start": (C.c_int, []),
     "xmg_timer_stop": (C.c_double, []),

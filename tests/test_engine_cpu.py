@@ -190,3 +190,27 @@ def test_invalid_indices_return_status(engine, pagefile):
     assert st == 1
     for t in (a, b, c):
         t.free()
+
+
+@pytest.mark.parametrize("dims", [[96, 384, 30, 17], [16, 31, 64, 1000], [5, 100, 128, 47]])
+def test_autosplit_tiles_opt_in(engine, dims):
+    """The opt-in tile-aware autosplit cuts every dimension at multiples of
+    the quantum into parts near the target; the default autosplit is left
+    as the reference's (its known answers are pinned elsewhere)."""
+    bs = api.BlockSpace(engine, dims)
+    try:
+        engine.check(engine.xmg_block_space_autosplit_tiles(bs.h, 32, 16))
+        nb = bs.nblocks()
+        for d, n in enumerate(dims):
+            sizes = [bs.block_dims([0] * d + [i] + [0] * (len(dims) - d - 1))[d]
+                     for i in range(nb[d])]
+            assert sum(sizes) == n
+            cuts = np.cumsum(sizes)[:-1]
+            assert all(c % 16 == 0 for c in cuts)
+            if n >= 16:
+                assert all(s >= 16 for s in sizes)
+                assert max(sizes) <= 2 * 32 + 15
+    finally:
+        bs.free()
+    with pytest.raises(api.XmError):
+        engine.check(engine.xmg_block_space_autosplit_tiles(None, 32, 16))
