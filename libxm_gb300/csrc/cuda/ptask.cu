@@ -99,7 +99,7 @@ outer_offsets(const xmgd_ptask_t &t, int first_dim, int64_t o, int64_t &od,
 }
 
 template <typename D, typename S, int MODE>
-__global__ void __launch_bounds__(PT_THREADS)
+__global__ void __launch_bounds__(PT_THREADS, (MODE == 0 || MODE == 3) ? 6 : 1)
 ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
     const task_meta *__restrict__ meta, int ntasks, int64_t cta0,
     double *__restrict__ partial)
