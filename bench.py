@@ -386,7 +386,7 @@ def engine_arm(args, ranks):
         writes = [(t.h, api.Dim.of(blk), host[(id(t), blk)][0])
                   for t in (w.a, w.b) for blk in t.canonical_blocks()]
         reads = [(w.c.h, api.Dim.of(blk), p) for blk, (p, n) in outs.items()]
-        phase = np.zeros(3)
+        phase = np.zeros(4)
 
         def e2e_step():
             t0 = time.perf_counter()
@@ -395,9 +395,10 @@ def engine_arm(args, ranks):
             t1 = time.perf_counter()
             w.run()
             t2 = time.perf_counter()
+            dev = api.last_stats(eng).ms_device
             for h, d, p in reads:
                 eng.xm_tensor_read_block(h, d, p)
-            phase[:] += (t1 - t0, t2 - t1, time.perf_counter() - t2)
+            phase[:] += (t1 - t0, t2 - t1, time.perf_counter() - t2, dev * 1e-3)
         e2e_step()
         ranks.barrier()
         phase[:] = 0
@@ -409,7 +410,8 @@ def engine_arm(args, ranks):
                "h2d_bytes_per_step": nbytes_in, "d2h_bytes_per_step": nbytes_out,
                "ms_per_step": dt * 1e3,
                "phases_ms": {"h2d": phase[0] * 1e3 / steps, "contract": phase[1] * 1e3 / steps,
-                             "d2h": phase[2] * 1e3 / steps},
+                             "d2h": phase[2] * 1e3 / steps,
+                             "contract_device": phase[3] * 1e3 / steps},
                "copies_per_step": len(writes) + len(reads)}
         for p, _ in host.values():
             eng.xmg_host_free(p)

@@ -844,6 +844,11 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			}
 		}
 	}
+	/* the producer, MMA and forwarder roles run on lane 0 alone: their
+	 * warps reconverge first, because an aligned barrier counts a whole
+	 * warp as arrived when any of its lanes arrives, and TMEM must stay
+	 * allocated until the MMA lane has seen its last commit land */
+	__syncwarp();
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();

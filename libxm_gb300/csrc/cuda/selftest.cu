@@ -24,6 +24,7 @@ selftest_wait_kernel(uint64_t limit_ns, int *flag)
 	__syncthreads();
 	if (threadIdx.x == 0)
 		mbar_wait_for(smem_u32(&bar), 0, &s_err, flag, 11, limit_ns);
+	__syncwarp();	/* lane 0 rejoins before the aligned barrier */
 	__syncthreads();
 }
 
