@@ -232,11 +232,10 @@ def block_costs(w):
 GEMM_DRAM_BYTES = 141.50e9 + 0.73965e9
 
 
-def timed_calls(eng, fn, reps=3):
-    """Device time per call of fn after one untimed call (plan, tuning)."""
-    fn()
-    fn()
-    fn()
+def timed_calls(eng, fn, reps=3, warm=3):
+    """Device time per call of fn after `warm` untimed calls (plan, tuning)."""
+    for _ in range(warm):
+        fn()
     eng.check(eng.xmg_synchronize())
     eng.check(eng.xmg_timer_start())
     for _ in range(reps):
@@ -300,8 +299,31 @@ def other_configs(eng, api, W):
         eng.check(eng.xm_contract_adjoint(api.Scalar.of(1.0), w.a.h, w.b.h, dc.h, da.h, db.h,
                                           b"ijcd", b"cdab", b"ijab"))
     ms = timed_calls(eng, adj)
-    out["cfg4_adjoint_cfg2"] = {"ms": ms, "tflops": 2 * fl / ms / 1e9, "useful_flops": 2 * fl,
-                                "note": "dA and dB: two contractions of the cfg2 size plus the folds"}
+
+    def grads():
+        api.set_all(da, 0)
+        api.set_all(db, 0)
+        adj()
+        return {**{("a",) + k: v for k, v in W.read_canonical(da).items()},
+                **{("b",) + k: v for k, v in W.read_canonical(db).items()}}
+    g_emu = grads()
+    used = api.last_stats(eng).precision_used
+    # the same adjoint on the FP64 path: one call (about 9 s)
+    eng.check(eng.xmg_set_precision(api.PREC_FP64))
+    try:
+        ms64 = timed_calls(eng, adj, reps=1, warm=1)
+        g_64 = grads()
+    finally:
+        eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+    out["cfg4_adjoint_cfg2"] = {
+        "ms": ms, "tflops": 2 * fl / ms / 1e9, "useful_flops": 2 * fl,
+        "precision_used": used,
+        "fp64_plain": {"ms": ms64, "tflops": 2 * fl / ms64 / 1e9},
+        "speedup_vs_fp64_plain": ms64 / ms,
+        "rel_err_vs_fp64": W.rel_frobenius(g_emu, g_64),
+        "note": "dA and dB in one call: the gradient contractions at every nonzero "
+                "position of A and B (about 4x the useful flops of the forward "
+                "pair), then the folds onto canonical blocks"}
     for x in (dc, da, db):
         x.free()
     w.free()
@@ -441,6 +463,7 @@ def engine_arm(args, ranks):
                "staged_bytes": st.stage_bytes, "stage_gbs": st.stage_bytes / dt / 1e9,
                "batches": st.stage_batches, "region_bytes": int(2e9),
                "device_ms": st.ms_device, "stage_wait_ms": st.ms_stage_wait,
+               "plan_ms": st.ms_plan,
                "precision_used": "emu64" if st.precision_used == api.PREC_EMU64 else "fp64",
                "note": "all tensors in a pagefile on the box's disk (page cache warm); "
                        "b streamed in batches, wall clock per xm_contract"}

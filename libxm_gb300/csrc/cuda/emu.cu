@@ -276,6 +276,43 @@ emu_split_kernel(const xmgd_view_t *__restrict__ views,
 /* ------------------------------------------------------------------ */
 /* 3. grouped tcgen05 GEMM with exact drains and the fused fold        */
 
+/* V * 2^e (sign flipped by sx) as a double, assembled in integer
+ * arithmetic: |V| rounded once to 53 bits (to nearest, ties to even), the
+ * exponent field written directly.  Bit-identical to ldexp((double)V, e)
+ * whenever the result is a normal number; false otherwise (the caller
+ * takes the FP64 path).  GB300's FP64 pipe is ~1/64 of its FP32 rate, so
+ * the epilogue keeps the conversion and the scaling off it. */
+__device__ __forceinline__ bool pack_f64(long long V, int e, unsigned long long sx,
+    double &out)
+{
+	if (V == 0) {
+		out = __longlong_as_double((long long)sx);
+		return true;
+	}
+	const unsigned long long sg = (V < 0 ? 1ull << 63 : 0ull) ^ sx;
+	const unsigned long long a = V < 0 ? 0ull - (unsigned long long)V :
+	    (unsigned long long)V;
+	int msb = 63 - __clzll((long long)a);
+	const int sh = msb - 52;
+	unsigned long long m;
+	if (sh > 0) {
+		const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+		m = a >> sh;
+		m += (rem > half) || (rem == half && (m & 1));
+		if (m >> 53) {
+			m >>= 1;
+			msb++;
+		}
+	} else
+		m = a << -sh;
+	const int be = msb + e + 1023;
+	if (be < 1 || be > 2046)
+		return false;
+	out = __longlong_as_double((long long)(sg | ((unsigned long long)be << 52) |
+	    (m & 0xFFFFFFFFFFFFFull)));
+	return true;
+}
+
 template <int S>
 struct stage_cfg {
 	static constexpr int CHUNK_BYTES = S * SLICE_BYTES;
@@ -345,7 +382,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ EA,
     const int32_t *__restrict__ EB, const int32_t *__restrict__ cbF,
-    double alpha, double beta, int expoff2, int cplx, int *__restrict__ flags)
+    double alpha, double beta, int expoff2, int cplx, int hmax,
+    int *__restrict__ flags)
 {
 	using C = stage_cfg<S>;
 	constexpr int NST = C::NST;
@@ -584,9 +622,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					for (int c0 = 0; c0 < nks && !s_err; ) {
 						const int c1 = chunk_end(c0, nks, cplx);
 						/* head: the first H (staged) steps; tail: the last T
-						 * steps; middle: the rest */
-						const int H = min(NST, c1 - c0);
-						const int T = min(NST, c1 - c0 - H);
+						 * steps; middle: the rest.  H, T <= hmax <= NST: the
+						 * stages a head or tail holds are released only after
+						 * its set-Y products, so hmax < NST leaves stages for
+						 * the producer to prefetch the steps after them */
+						const int H = min(hmax, c1 - c0);
+						const int T = min(hmax, c1 - c0 - H);
 						/* every accumulator restarts each chunk: the exact
 						 * groups for their 2^23 bound, the low band because
 						 * the tensor core's fp32 accumulation error grows
@@ -831,12 +872,24 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				const int fe = (swp ? EA + cb.eA : EB + cb.eB)[ms];
 				const bool bz = beta == 0.0;
 				const int cm = cplx ? 2 : 1;
+				/* alpha a normal power of two folds into the exponent
+				 * and sign; any other alpha costs one multiply */
+				const long long ab = __double_as_longlong(alpha);
+				const int aex = (int)((ab >> 52) & 0x7ff);
+				const bool apow2 = (ab & 0xFFFFFFFFFFFFFll) == 0 && aex > 0 && aex < 0x7ff;
+				const int esh = apow2 ? aex - 1023 : 0;
+				const unsigned long long asx = apow2 ?
+				    (unsigned long long)ab & (1ull << 63) : 0ull;
 #pragma unroll
 				for (int c = 0; c < NC; c++) {
 					const int q = q0 + c;
 					if (q < vlim) {
 						const int e = vexp[q] + fe - expoff2 - 16 - F;
-						double v = alpha * ldexp((double)V[c], e);
+						double v;
+						if (!pack_f64(V[c], e + esh, asx, v))
+							v = alpha * ldexp((double)V[c], e);
+						else if (!apow2)
+							v *= alpha;
 						TOUT *cp = Cp + (size_t)cm * (vtab[q] + fo) + pass;
 						*cp = bz ? (TOUT)v : (TOUT)fma(beta, (double)*cp, v);
 					}
@@ -949,6 +1002,7 @@ struct emu_plan {
 	const int32_t *d_tabs;
 	std::vector<emu_cand> cand;
 	int cur = 0, tuned = 0;
+	int hmax = 4;                        /* head/tail steps (<= stages) */
 	uint64_t sig = 0;
 	int *h_flags = nullptr;              /* pinned: Inf/NaN, timeout */
 	int (*split)(emu_plan *) = nullptr;
@@ -1019,14 +1073,14 @@ launch_gemm(emu_plan *e)
 		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    (const int32_t *)EA, (const int32_t *)EB, (const int32_t *)e->d_F,
-		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, flags));
+		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags));
 	} else {
 		emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, false><<<(unsigned)c.grid,
 		    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
 		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
-		    2 * fin<TIN>::EXPOFF, e->cplx, flags);
+		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags);
 	}
 	g_launches++;
 	XMG_CK(cudaGetLastError());
@@ -1186,6 +1240,12 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	emu_plan *e = new emu_plan();
 	e->dtype = p->dtype;
 	e->cplx = cplx;
+	{
+		const int nst = dbl ? stage_cfg<fin<double>::S>::NST : stage_cfg<fin<float>::S>::NST;
+		const char *h = getenv("XMG_EMU_HEAD");
+		e->hmax = h ? atoi(h) : 4;
+		e->hmax = std::max(1, std::min(nst, e->hmax));
+	}
 	e->alpha = p->alpha[0];
 	e->beta = p->beta[0];
 	e->d_cbs = d_cbs;

@@ -244,6 +244,18 @@ xmgd_side_copy(int slot, uint64_t dst, size_t bytes)
 	return XMG_OK;
 }
 
+/* the reverse: device bytes into chunk `slot` (write-back of staged
+ * views); side_wait(slot) then makes the chunk readable */
+extern "C" int
+xmgd_side_fetch(int slot, uint64_t src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync(g_chunk[slot].p, (const void *)(uintptr_t)src, bytes,
+	    cudaMemcpyDeviceToHost, g_side));
+	XMG_CK(cudaEventRecord(g_side_ev[slot], g_side));
+	g_side_rec[slot] = true;
+	return XMG_OK;
+}
+
 extern "C" int
 xmgd_side_sync(void)
 {

@@ -33,6 +33,8 @@ struct xm_allocator {
 	xmg_hmap_t views;         /* pagefile: handle -> staged device addr */
 	xmg_hmap_t stream;        /* pagefile: handle -> address in the
 	                             current out-of-core batch */
+	xmg_hmap_t bviews;        /* pagefile: handle -> view inside `bulk` */
+	uint64_t bulk;            /* one HBM buffer holding the bulk views */
 };
 
 static int bit_get(const unsigned char *b, uint64_t i) { return (b[i >> 3] >> (i & 7)) & 1; }
@@ -57,6 +59,7 @@ xm_allocator_create(const char *path)
 	xmg_hmap_init(&a->live);
 	xmg_hmap_init(&a->views);
 	xmg_hmap_init(&a->stream);
+	xmg_hmap_init(&a->bviews);
 	a->fd = -1;
 	if (path == NULL) {
 		if (xmgd_init() != XMG_OK) {
@@ -245,7 +248,8 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 		return XMG_OK;
 	}
 	if (xmg_hmap_get(&a->stream, h, dptr) ||
-	    xmg_hmap_get(&a->views, h, dptr))
+	    xmg_hmap_get(&a->views, h, dptr) ||
+	    xmg_hmap_get(&a->bviews, h, dptr))
 		return XMG_OK;
 	if ((st = xmgd_alloc(bytes, &d)) != XMG_OK)
 		return st;
@@ -273,7 +277,7 @@ xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes)
 
 	if (a->path == NULL)
 		return XMG_OK;
-	if (!xmg_hmap_get(&a->views, h, &d))
+	if (!xmg_hmap_get(&a->views, h, &d) && !xmg_hmap_get(&a->bviews, h, &d))
 		return xmg_seterr(XMG_EINVAL, "no staged view for handle");
 	if ((st = xmgd_pinned(bytes, &pin)) != XMG_OK ||
 	    (st = xmgd_d2h(pin, d, bytes)) != XMG_OK)
@@ -294,7 +298,44 @@ xmg_alloc_release_views(xm_allocator_t *a, int write_back)
 			xmgd_free(a->views.vals[i]);
 	xmg_hmap_free(&a->views);
 	xmg_hmap_init(&a->views);
+	if (a->bulk)
+		xmgd_free(a->bulk);
+	a->bulk = 0;
+	xmg_hmap_free(&a->bviews);
+	xmg_hmap_init(&a->bviews);
 	return XMG_OK;
+}
+
+/* Views staged together: the blocks h[i] live at d[i] inside the HBM
+ * buffer `bulk` (filled by the caller), which the allocator takes over in
+ * every case (freed here on error, else with the other views). */
+int
+xmg_alloc_bulk_views(xm_allocator_t *a, uint64_t bulk, const uint64_t *h,
+    const uint64_t *d, size_t n)
+{
+	size_t i;
+
+	if (a->path == NULL || a->bulk) {
+		xmgd_free(bulk);
+		return xmg_seterr(XMG_EINVAL, "bulk views: pagefile allocator "
+		    "without bulk views expected");
+	}
+	a->bulk = bulk;
+	for (i = 0; i < n; i++)
+		if (xmg_hmap_put(&a->bviews, h[i], d[i]))
+			return xmg_seterr(XMG_ENOMEM, "out of memory");
+	return XMG_OK;
+}
+
+/* device address of a staged view (either kind), 0 if none */
+uint64_t
+xmg_alloc_view_addr(const xm_allocator_t *a, uint64_t h)
+{
+	uint64_t d;
+
+	if (xmg_hmap_get(&a->views, h, &d) || xmg_hmap_get(&a->bviews, h, &d))
+		return d;
+	return 0;
 }
 
 /* Out-of-core batches: while set, blocks of the batch resolve to their
@@ -342,6 +383,7 @@ xm_allocator_destroy(xm_allocator_t *a)
 	xmg_hmap_free(&a->live);
 	xmg_hmap_free(&a->views);
 	xmg_hmap_free(&a->stream);
+	xmg_hmap_free(&a->bviews);
 	free(a->path);
 	free(a->used);
 	free(a);
@@ -359,4 +401,18 @@ xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
 		return xmgd_d2h(mem, h + byte_off, bytes);
 	r = pread(a->fd, mem, bytes, page_offset(h) + (off_t)byte_off);
 	return r == (ssize_t)bytes ? XMG_OK : xmg_seterr(XMG_EIO, "pread");
+}
+
+/* Write part of a pagefile block (byte range) from host memory. */
+int
+xmg_alloc_write_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
+    const void *mem, size_t bytes)
+{
+	ssize_t r;
+
+	if (a->path == NULL)
+		return xmg_seterr(XMG_EINVAL, "write_range: pagefile allocator "
+		    "expected");
+	r = pwrite(a->fd, mem, bytes, page_offset(h) + (off_t)byte_off);
+	return r == (ssize_t)bytes ? XMG_OK : xmg_seterr(XMG_EIO, "pwrite");
 }

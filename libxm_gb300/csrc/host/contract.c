@@ -628,14 +628,17 @@ xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
 
 /*
  * b's pagefile blocks are streamed through two HBM regions: reader threads
- * (XMG_STAGE_THREADS, default 8) read batch i+1 from the pagefile into
+ * (XMG_STAGE_THREADS, default 12) read batch i+1 from the pagefile into
  * pinned 64 MiB chunks, two per reader used in turn, and copy each on the
  * side stream (cudaMemcpyAsync) into the idle region while batch i is
  * contracted on the compute stream.  Each batch is an
  * ordinary contraction restricted to the merged pairs whose b data lies in
  * the batch (pairs merge only over equal b data, so the restriction
  * commutes with merging); beta is applied by the first batch and the later
- * ones accumulate with beta = 1.
+ * ones accumulate with beta = 1.  a's and c's canonical blocks are staged
+ * whole, as views in one HBM buffer, by the same readers together with
+ * batch 0 while batch 0's plan is built; c is written back by them in
+ * reverse (side-stream fetches into the pinned chunks, pwrite).
  */
 #define STAGE_CHUNK ((size_t)64 << 20)
 #define STAGE_ALIGN 256
@@ -660,18 +663,21 @@ xmg_set_staging(size_t budget, size_t region)
 	return XMG_OK;
 }
 
+/* a list of pagefile blocks moved by the reader threads: block i is
+ * h[i] (sz[i] bytes) in the pagefile and dst[i] in HBM; wr = 0 reads the
+ * pagefile into HBM, wr = 1 writes HBM back to the pagefile */
 struct io_job {
 	xm_allocator_t *al;
-	const uint64_t *h, *sz, *off;
+	const uint64_t *h, *sz, *dst;
 	size_t n;
-	uint64_t region;
+	int wr;
 	int status;
 	char err[256];
 	pthread_t th;
 	int running;
 };
 
-/* one reader: chunks w, w + nw, w + 2 nw, ... of the batch, alternating
+/* one reader: chunks w, w + nw, w + 2 nw, ... of the list, alternating
  * its two pinned slots */
 struct io_worker {
 	struct io_job *j;
@@ -688,19 +694,39 @@ io_worker_main(void *arg)
 	void *buf;
 	int st = xmgd_bind_thread();
 
+	/* write-back: the chunk fetched last is written while the next one
+	 * is fetched */
+	int pslot = -1;
+	size_t pi = 0, po = 0, pn = 0;
+	void *pbuf = NULL;
+
 	for (i = 0; st == XMG_OK && i < j->n; i++)
 		for (o = 0; st == XMG_OK && o < j->sz[i]; o += n, k++) {
 			n = j->sz[i] - o < STAGE_CHUNK ? j->sz[i] - o : STAGE_CHUNK;
 			if ((int)(k % (size_t)r->nw) != r->w)
 				continue;
 			const int slot = 2 * r->w + (int)(mine++ & 1);
-			/* a chunk is refilled only after its previous copy */
-			if ((st = xmgd_side_wait(slot)) == XMG_OK &&
-			    (st = xmgd_side_chunk(slot, STAGE_CHUNK, &buf)) == XMG_OK &&
-			    (st = xmg_alloc_read_range(j->al, j->h[i], o, buf, n)) ==
-			    XMG_OK)
-				st = xmgd_side_copy(slot, j->region + j->off[i] + o, n);
+			if (!j->wr) {
+				/* a chunk is refilled only after its previous copy */
+				if ((st = xmgd_side_wait(slot)) == XMG_OK &&
+				    (st = xmgd_side_chunk(slot, STAGE_CHUNK, &buf)) == XMG_OK &&
+				    (st = xmg_alloc_read_range(j->al, j->h[i], o, buf, n)) ==
+				    XMG_OK)
+					st = xmgd_side_copy(slot, j->dst[i] + o, n);
+				continue;
+			}
+			/* the slot's previous chunk went out one round ago */
+			if ((st = xmgd_side_chunk(slot, STAGE_CHUNK, &buf)) != XMG_OK ||
+			    (st = xmgd_side_fetch(slot, j->dst[i] + o, n)) != XMG_OK)
+				break;
+			if (pslot >= 0 && ((st = xmgd_side_wait(pslot)) != XMG_OK ||
+			    (st = xmg_alloc_write_range(j->al, j->h[pi], po, pbuf, pn)) !=
+			    XMG_OK))
+				break;
+			pslot = slot; pi = i; po = o; pn = n; pbuf = buf;
 		}
+	if (st == XMG_OK && pslot >= 0 && (st = xmgd_side_wait(pslot)) == XMG_OK)
+		st = xmg_alloc_write_range(j->al, j->h[pi], po, pbuf, pn);
 	r->status = st;
 	if (st != XMG_OK)
 		snprintf(r->err, sizeof r->err, "%s", xmg_last_error());
@@ -711,7 +737,7 @@ static int
 stage_threads(void)
 {
 	const char *e = getenv("XMG_STAGE_THREADS");
-	int n = e ? atoi(e) : 8;
+	int n = e ? atoi(e) : 12;
 
 	return n < 1 ? 1 : n > XMGD_SIDE_SLOTS / 2 ? XMGD_SIDE_SLOTS / 2 : n;
 }
@@ -813,24 +839,117 @@ fill_contract(xmgd_contract_t *dp, const plan_t *p, xm_scalar_t alpha,
 	dp->emulatable = p->emulatable;
 }
 
-/* Write c's staged views back to its pagefile and drop every view. */
+/* Write c's staged views back to its pagefile (the reader threads in
+ * reverse: side-stream fetches into pinned chunks, pwrite) and drop every
+ * view. */
 static int
 commit_c(xm_tensor_t *c, int st)
 {
 	xm_dim_t *list;
-	size_t n, q;
+	size_t n, q, m = 0;
+	uint64_t *h = NULL, *sz = NULL, *d = NULL;
+	struct io_job j;
 
 	if (xmg_alloc_is_device(c->allocator))
 		return st;
 	if (st == XMG_OK) {
 		xm_tensor_get_canonical_block_list(c, &list, &n);
-		for (q = 0; q < n && st == XMG_OK; q++)
-			st = xmg_alloc_commit_view(c->allocator,
-			    xm_tensor_get_block_data_ptr(c, list[q]),
-			    xm_tensor_get_block_bytes(c, list[q]));
+		h = malloc((n + 1) * sizeof *h);
+		sz = malloc((n + 1) * sizeof *sz);
+		d = malloc((n + 1) * sizeof *d);
+		if (!h || !sz || !d)
+			xm_fatal("%s: out of memory", __func__);
+		for (q = 0; q < n; q++) {
+			h[m] = xm_tensor_get_block_data_ptr(c, list[q]);
+			sz[m] = xm_tensor_get_block_bytes(c, list[q]);
+			d[m] = xmg_alloc_view_addr(c->allocator, h[m]);
+			if (d[m] == 0) {
+				st = xmg_seterr(XMG_EINVAL, "xm_contract: output block "
+				    "without a staged view");
+				break;
+			}
+			m++;
+		}
 		free(list);
+		if (st == XMG_OK && m > 0) {
+			memset(&j, 0, sizeof j);
+			j.al = c->allocator;
+			j.h = h; j.sz = sz; j.dst = d; j.n = m; j.wr = 1;
+			if ((st = io_start(&j)) == XMG_OK)
+				st = io_join(&j);
+		}
+		free(h); free(sz); free(d);
 	}
 	xmg_alloc_release_views(c->allocator, 0);
+	return st;
+}
+
+/*
+ * Views of a's and c's canonical blocks (one pagefile allocator) in one
+ * HBM buffer, registered with the allocator; returns the blocks to read
+ * into them (c's only when read_c: for beta = 0 the contraction
+ * overwrites c, as the reference zeroes it, contract.c:155-158).
+ */
+static int
+bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
+    uint64_t **rh, uint64_t **rsz, uint64_t **rd, size_t *nr)
+{
+	const xm_tensor_t *t[2] = {a, c};
+	xm_dim_t *list[2] = {NULL, NULL};
+	size_t n[2] = {0, 0}, cnt = 0, m = 0, q, s;
+	uint64_t *h, *sz, *d, off = 0, bulk = 0;
+	char *rdf;
+	xmg_hmap_t seen;
+	int st = XMG_OK;
+
+	for (s = 0; s < 2; s++) {
+		xm_tensor_get_canonical_block_list(t[s], &list[s], &n[s]);
+		cnt += n[s];
+	}
+	h = malloc((cnt + 1) * sizeof *h);
+	sz = malloc((cnt + 1) * sizeof *sz);
+	d = malloc((cnt + 1) * sizeof *d);
+	rdf = malloc(cnt + 1);
+	if (!h || !sz || !d || !rdf)
+		xm_fatal("%s: out of memory", __func__);
+	xmg_hmap_init(&seen);
+	for (s = 0; s < 2; s++)
+		for (q = 0; q < n[s]; q++) {
+			uint64_t hq = xm_tensor_get_block_data_ptr(t[s], list[s][q]), v;
+			if (xmg_hmap_get(&seen, hq, &v)) {
+				rdf[v] |= s == 0 || read_c;
+				continue;
+			}
+			if (xmg_hmap_put(&seen, hq, m))
+				xm_fatal("%s: out of memory", __func__);
+			h[m] = hq;
+			sz[m] = xm_tensor_get_block_bytes(t[s], list[s][q]);
+			d[m] = off;
+			rdf[m] = s == 0 || read_c;
+			off += (sz[m] + STAGE_ALIGN - 1) / STAGE_ALIGN * STAGE_ALIGN;
+			m++;
+		}
+	xmg_hmap_free(&seen);
+	free(list[0]);
+	free(list[1]);
+	if (m > 0 && (st = xmgd_alloc(off, &bulk)) == XMG_OK) {
+		for (q = 0; q < m; q++)
+			d[q] += bulk;
+		st = xmg_alloc_bulk_views(a->allocator, bulk, h, d, m);
+	}
+	/* keep the blocks to read, in order */
+	*nr = 0;
+	for (q = 0; st == XMG_OK && q < m; q++)
+		if (rdf[q]) {
+			h[*nr] = h[q];
+			sz[*nr] = sz[q];
+			d[*nr] = d[q];
+			(*nr)++;
+		}
+	free(rdf);
+	*rh = h;
+	*rsz = sz;
+	*rd = d;
 	return st;
 }
 
@@ -847,6 +966,9 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	plan_t p0;
 	struct hsz *u = NULL;
 	uint64_t *H = NULL, *SZ = NULL, *OFF = NULL, *D = NULL, total = 0;
+	uint64_t *VH = NULL, *VSZ = NULL, *VD = NULL, *JH = NULL, *JSZ = NULL,
+	    *JD = NULL;
+	size_t nv = 0;
 	uint64_t reg[2] = {0, 0}, rbytes = 0, run;
 	size_t budget, region, nu = 0, i, *bstart = NULL, nb = 0, k;
 	struct io_job io[2];
@@ -926,11 +1048,29 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		goto out_free;
 	for (k = 0; k < 2; k++)
 		io[k].al = b->allocator;
-	/* batch 0 first, synchronously */
-	io[0].h = H; io[0].sz = SZ; io[0].off = OFF;
-	io[0].n = bstart[1];
-	io[0].region = reg[0];
-	if ((*st = io_start(&io[0])) != XMG_OK || (*st = io_join(&io[0])) != XMG_OK)
+	/* every b block's address in its batch's region */
+	for (k = 0; k < nb; k++)
+		for (i = bstart[k]; i < bstart[k + 1]; i++)
+			D[i] = reg[k & 1] + OFF[i];
+	/* a's and c's blocks as views in one buffer, read together with
+	 * batch 0 while batch 0's plan is built (plans need addresses only) */
+	if ((*st = bulk_views(a, c, creal(beta) != 0 || cimag(beta) != 0, &VH,
+	    &VSZ, &VD, &nv)) != XMG_OK)
+		goto out_free;
+	JH = malloc((nv + bstart[1] + 1) * sizeof *JH);
+	JSZ = malloc((nv + bstart[1] + 1) * sizeof *JSZ);
+	JD = malloc((nv + bstart[1] + 1) * sizeof *JD);
+	if (!JH || !JSZ || !JD)
+		xm_fatal("%s: out of memory", __func__);
+	memcpy(JH, VH, nv * sizeof *JH);
+	memcpy(JSZ, VSZ, nv * sizeof *JSZ);
+	memcpy(JD, VD, nv * sizeof *JD);
+	memcpy(JH + nv, H, bstart[1] * sizeof *JH);
+	memcpy(JSZ + nv, SZ, bstart[1] * sizeof *JSZ);
+	memcpy(JD + nv, D, bstart[1] * sizeof *JD);
+	io[0].h = JH; io[0].sz = JSZ; io[0].dst = JD;
+	io[0].n = nv + bstart[1];
+	if ((*st = io_start(&io[0])) != XMG_OK)
 		goto out_free;
 	tw = 0;
 	for (k = 0; k < nb && *st == XMG_OK; k++) {
@@ -939,24 +1079,13 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		xmgd_plan_t *hp = NULL;
 		plan_t p;
 		int used = XMG_PREC_FP64;
-		double t0;
+		double t0 = now_ms();
 
-		if (k + 1 < nb) {
-			nx->h = H + bstart[k + 1];
-			nx->sz = SZ + bstart[k + 1];
-			nx->off = OFF + bstart[k + 1];
-			nx->n = bstart[k + 2] - bstart[k + 1];
-			nx->region = reg[(k + 1) & 1];
-			if ((*st = io_start(nx)) != XMG_OK)
-				break;
-		}
 		/* the batch's blocks resolve into its region */
 		xmg_hmap_free(&filt);
 		xmg_hmap_init(&filt);
-		for (i = bstart[k]; i < bstart[k + 1]; i++) {
-			D[i] = reg[k & 1] + OFF[i];
+		for (i = bstart[k]; i < bstart[k + 1]; i++)
 			xmg_hmap_put(&filt, H[i], 1);
-		}
 		if ((*st = xmg_alloc_stream_set(b->allocator, H + bstart[k],
 		    D + bstart[k], bstart[k + 1] - bstart[k])) != XMG_OK)
 			break;
@@ -965,11 +1094,31 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		if ((*st = check_contract(a, b, c, idxa, idxb, idxc, &p)) ==
 		    XMG_OK && (*st = build_plan(alpha, a, b, c, &p, 1)) == XMG_OK) {
 			fill_contract(&dp, &p, alpha, k == 0 ? beta : 1, prec);
-			if ((*st = xmgd_plan_create(&dp, &hp)) == XMG_OK) {
-				*st = xmgd_plan_run(hp, &used);
-				xmgd_plan_free(hp);
-			}
+			*st = xmgd_plan_create(&dp, &hp);
 		}
+		acc.ms_plan += now_ms() - t0;
+		/* batch k's data in place (only batch 0 can still be loading:
+		 * later batches were joined at the end of the previous round),
+		 * then batch k + 1 streams in while batch k is contracted; one
+		 * job at a time, as the readers share the pinned slots */
+		if (k == 0) {
+			t0 = now_ms();
+			int s2 = io_join(&io[0]);
+			tw += now_ms() - t0;
+			if (*st == XMG_OK)
+				*st = s2;
+		}
+		if (*st == XMG_OK && k + 1 < nb) {
+			nx->h = H + bstart[k + 1];
+			nx->sz = SZ + bstart[k + 1];
+			nx->dst = D + bstart[k + 1];
+			nx->n = bstart[k + 2] - bstart[k + 1];
+			*st = io_start(nx);
+		}
+		if (*st == XMG_OK)
+			*st = xmgd_plan_run(hp, &used);
+		if (hp)
+			xmgd_plan_free(hp);
 		if (*st == XMG_OK) {
 			xmgd_timing_t tm;
 			xmgd_last_timing(&tm);
@@ -1019,6 +1168,7 @@ out_free:
 	xmg_alloc_release_views(a->allocator, 0);
 out:
 	free(u); free(H); free(SZ); free(OFF); free(D); free(bstart);
+	free(VH); free(VSZ); free(VD); free(JH); free(JSZ); free(JD);
 	return 1;
 }
 

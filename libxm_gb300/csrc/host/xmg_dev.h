@@ -28,13 +28,15 @@ int xmgd_scratch(int slot, size_t bytes, uint64_t *dptr);
 int xmgd_pinned(size_t bytes, void **hptr);
 /* Out-of-core staging on the side stream: pinned chunk buffers in
  * XMGD_SIDE_SLOTS slots (two per reader thread); side_copy sends chunk
- * `slot` to dst asynchronously, side_wait blocks until that slot's last
- * copy is done (the buffer may then be refilled), side_sync drains the
- * side stream.  Distinct slots may be used from distinct threads. */
-#define XMGD_SIDE_SLOTS 16
+ * `slot` to dst asynchronously, side_fetch fills it from src, side_wait
+ * blocks until that slot's last copy is done (the buffer may then be
+ * reused), side_sync drains the side stream.  Distinct slots may be used
+ * from distinct threads. */
+#define XMGD_SIDE_SLOTS 32
 int xmgd_bind_thread(void);
 int xmgd_side_chunk(int slot, size_t bytes, void **hptr);
 int xmgd_side_copy(int slot, uint64_t dst, size_t bytes);
+int xmgd_side_fetch(int slot, uint64_t src, size_t bytes);
 int xmgd_side_wait(int slot);
 int xmgd_side_sync(void);
 size_t xmgd_arena_bytes_in_use(void);

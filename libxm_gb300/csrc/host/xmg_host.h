@@ -71,6 +71,11 @@ static inline void xmg_scalar_pack(xm_scalar_t s, double out[2])
 
 int xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
     void *mem, size_t bytes);
+int xmg_alloc_write_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
+    const void *mem, size_t bytes);
+int xmg_alloc_bulk_views(xm_allocator_t *a, uint64_t bulk, const uint64_t *h,
+    const uint64_t *d, size_t n);
+uint64_t xmg_alloc_view_addr(const xm_allocator_t *a, uint64_t h);
 int xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes);
 int xmg_alloc_stream_set(xm_allocator_t *a, const uint64_t *h,
     const uint64_t *d, size_t n);
