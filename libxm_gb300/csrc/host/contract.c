@@ -954,9 +954,10 @@ bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
 }
 
 /*
- * Out-of-core path.  Returns 0 when the contraction should run in core
- * (b in GPU memory, b aliasing a or c, or b's blocks within the budget),
- * else 1 with the status in *st.
+ * Pagefile path.  Returns 0 when the contraction should run through the
+ * in-core path (b in GPU memory or b aliasing a or c), else 1 with the
+ * status in *st.  b is streamed in batches when its blocks exceed the
+ * staging budget, else staged whole as a single batch.
  */
 static int
 contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
@@ -1006,10 +1007,10 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	for (i = 0; i < nu; i++)
 		total += u[i].sz;
 	plan_free(&p0);
-	if (total <= budget) {
-		free(u);
-		return 0;
-	}
+	/* within the budget b is staged whole: one batch, still read by the
+	 * parallel readers */
+	if (total <= budget)
+		region = total + nu * STAGE_ALIGN;
 	/* batches of at most `region` bytes (256-byte aligned offsets) */
 	H = malloc(nu * sizeof *H);
 	SZ = malloc(nu * sizeof *SZ);
