@@ -331,6 +331,54 @@ def other_configs(eng, api, W):
     return out
 
 
+def cfg5_subset(eng, api, W, v_blocks=12):
+    """The production ladder's structure (o = 128 as 8 x 16, v blocks of
+    24..40 with Z2^3 labels) on its first v_blocks v blocks, all tensors in
+    a pagefile and b streamed through two 2 GB regions: split-precision
+    against the plain FP64 path on the same inputs, wall clock per
+    xm_contract.  The full b (~275 GB) exceeds the host's disk and RAM."""
+    import tempfile
+    tmp = tempfile.mkdtemp(prefix="xmg_cfg5_")
+    pal = api.Allocator(eng, os.path.join(tmp, "pagefile"))
+    t0 = time.perf_counter()
+    w = W.cfg5(eng, pal, v_blocks=v_blocks)
+    setup = time.perf_counter() - t0
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(),
+                                w.idxc.encode())
+    nb = sum(w.b.block_size(blk) for blk in w.b.canonical_blocks()) * 8
+    out = {"workload": w.name, "v_blocks": v_blocks, "b_bytes": nb, "useful_flops": fl,
+           "setup_s": setup}
+    eng.check(eng.xmg_set_staging(1, int(2e9)))
+    try:
+        res = {}
+        for prec, name, reps in ((api.PREC_AUTO, "emu", 2), (api.PREC_FP64, "fp64", 1)):
+            eng.check(eng.xmg_set_precision(prec))
+            if prec == api.PREC_AUTO:
+                w.run()
+            best = 1e30
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                w.run()
+                best = min(best, time.perf_counter() - t0)
+            st = api.last_stats(eng)
+            res[name] = W.read_canonical(w.c)
+            out[name] = {"ms": best * 1e3, "tflops": fl / best / 1e12,
+                         "device_ms": st.ms_device, "batches": st.stage_batches,
+                         "stage_gbs": st.stage_bytes / best / 1e9,
+                         "precision_used": "emu64" if st.precision_used == api.PREC_EMU64
+                         else "fp64"}
+        out["speedup_vs_fp64_plain"] = out["fp64"]["ms"] / out["emu"]["ms"]
+        out["device_speedup_vs_fp64_plain"] = out["fp64"]["device_ms"] / out["emu"]["device_ms"]
+        out["rel_err_vs_fp64"] = W.rel_frobenius(res["emu"], res["fp64"])
+    finally:
+        eng.check(eng.xmg_set_precision(api.PREC_AUTO))
+        eng.check(eng.xmg_set_staging(int(180e9), int(32e9)))
+        w.free()
+        pal.destroy()
+        os.rmdir(tmp)
+    return out
+
+
 def make_workload(lib, al, scale=1, subset=None):
     from libxm_gb300 import workloads as W
     ob, vb = (int(x) for x in subset.split(",")) if subset else (None, None)
@@ -471,6 +519,7 @@ def engine_arm(args, ranks):
         wp.free()
         pal.destroy()
         os.rmdir(tmp)
+        ooc["cfg5_subset"] = cfg5_subset(eng, api, W)
 
     configs = None if args.no_configs or ranks.rank != 0 else other_configs(eng, api, W)
 

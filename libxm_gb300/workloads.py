@@ -206,6 +206,31 @@ def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None):
     return w
 
 
+def cfg5_shape(seed=5):
+    o = [16] * 8
+    v = uneven_sizes(1024, 32, 24, 40, seed * 7 + 12)
+    lo = labels(8, seed * 7 + 13)
+    lv = labels(32, seed * 7 + 14)
+    return o, v, lo, lv
+
+
+def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None):
+    """Production ladder: o = 128 in 8 blocks of 16, v = 1024 in 32 blocks
+    of 24..40, Z2^3 labels.  The full b (vvvv) holds ~275 GB of canonical
+    data; v_blocks keeps the first v blocks only (block sizes and labels
+    unchanged) and scale > 1 shrinks every block size by that factor."""
+    o, v, lo, lv = cfg5_shape(seed)
+    if scale > 1:
+        o = [max(1, x // scale) for x in o]
+        v = [max(1, x // scale) for x in v]
+    if v_blocks:
+        v, lv = v[:v_blocks], lv[:v_blocks]
+    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv))
+    w.name = "cfg5_ladder_o%d_v%d_z2%s" % (sum(o), sum(v), "" if scale == 1 else "_scaled_%d" % scale)
+    w.extra = {"o_sizes": o, "v_sizes": v, "o_labels": lo, "v_labels": lv}
+    return w
+
+
 def cfg3(lib, alloc, dtype=api.FLOAT, seed=3, o_blk=16, v_blk=32, no=4, nv=8):
     """Ring term C(i,a,j,b) += sum_{k,c} A(k,i,c,a) B(j,k,b,c), beta = 1,
     C prefilled; (i,a) <-> (j,b) pair symmetry (+1) on C only, A and B

@@ -113,3 +113,29 @@ def test_block_larger_than_region(engine, pagefile):
     finally:
         engine.check(engine.xmg_set_staging(int(180e9), int(32e9)))
         w.free()
+
+
+def test_production_ladder_streamed(engine, oracle, staging, pagefile):
+    """The production ladder's structure (o = 128 as 8 x 16, v blocks of
+    24..40, Z2^3 labels) with block sizes divided by 4 and its first 10 v
+    blocks, b streamed in batches, against the oracle in both precision
+    modes; the two modes also agree with each other."""
+    oal = api.Allocator(oracle)
+    we = W.cfg5(engine, pagefile, scale=4, v_blocks=10)
+    wo = W.cfg5(oracle, oal, scale=4, v_blocks=10)
+    try:
+        wo.run()
+        ref = W.read_canonical(wo.c)
+        got = {}
+        for prec in (api.PREC_AUTO, api.PREC_FP64):
+            engine.check(engine.xmg_set_precision(prec))
+            we.run()
+            st = api.last_stats(engine)
+            assert st.stage_batches > 1
+            got[prec] = W.read_canonical(we.c)
+            assert W.rel_frobenius(got[prec], ref) <= REL, prec
+        assert W.rel_frobenius(got[api.PREC_AUTO], got[api.PREC_FP64]) <= REL
+    finally:
+        engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+        we.free()
+        wo.free()
