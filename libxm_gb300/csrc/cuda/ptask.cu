@@ -35,9 +35,43 @@ constexpr int PT_THREADS = 256;
 constexpr int ROW_ELEMS = 4096;    /* elements per CTA in row mode */
 constexpr int FLAT_ELEMS = 8192;   /* elements per CTA in flat mode */
 constexpr int TILE = 32;
-/* matrix mode: whole s0 x s1 slices (both <= MT) per CTA */
-template <typename S> struct mt_of { static constexpr int v = sizeof(S) <= 8 ? 64 : 32; };
+/* matrix mode: whole s0 x s1 slices (both <= MT) per CTA; a source and a
+ * destination tile of both types fit the 48 KB of static shared memory */
+template <typename D, typename S> struct mt_of {
+	static constexpr int v = sizeof(S) <= 8 && sizeof(D) <= 8 ? 48 : 32;
+};
+static inline int mt_host(int dbytes, int sbytes)
+{
+	return sbytes <= 8 && dbytes <= 8 ? 48 : 32;
+}
 constexpr int MAT_MAXQ = 64;       /* slices per CTA at most */
+
+/* asynchronous global -> shared copy of one element (cp.async: no
+ * register holds the value while it is in flight) */
+template <int B> __device__ __forceinline__ void cp_async_b(void *s, const void *g);
+template <> __device__ __forceinline__ void cp_async_b<4>(void *s, const void *g)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4;"
+	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
+}
+template <> __device__ __forceinline__ void cp_async_b<8>(void *s, const void *g)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
+	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
+}
+template <> __device__ __forceinline__ void cp_async_b<16>(void *s, const void *g)
+{
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
+}
+template <typename T> __device__ __forceinline__ void cp_async_elem(T *s, const T *g)
+{
+	cp_async_b<sizeof(T)>(s, g);
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+	asm volatile("cp.async.wait_all;" ::: "memory");
+}
 
 struct task_meta {
 	int64_t first_cta;
@@ -99,7 +133,7 @@ outer_offsets(const xmgd_ptask_t &t, int first_dim, int64_t o, int64_t &od,
 }
 
 template <typename D, typename S, int MODE>
-__global__ void __launch_bounds__(PT_THREADS, (MODE == 0 || MODE == 3) ? 6 : 1)
+__global__ void __launch_bounds__(PT_THREADS, MODE == 0 ? 6 : MODE == 3 ? 5 : 1)
 ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
     const task_meta *__restrict__ meta, int ntasks, int64_t cta0,
     double *__restrict__ partial)
@@ -202,11 +236,15 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		}
 	} else if constexpr (MODE == 3) {
 		/* matrix: whole s0 x s1 slices (dim 0 unit-stride in dst, dim 1
-		 * in src); rows_per_cta slices per CTA, packed in shared memory
-		 * with row pitch s0 + 1 and moved together: all loads of the
-		 * group in flight, then all stores */
-		constexpr int MT = mt_of<S>::v;
-		__shared__ S mtile[MT * (MT + 1)];
+		 * in src); rows_per_cta slices per CTA.  Every load of the CTA is
+		 * in flight at once as a cp.async copy: the source transposed
+		 * into a padded tile (row pitch s0 + 1), the destination (when
+		 * the op reads it) into a second tile in its own order; one wait;
+		 * then the op from shared memory and stores along the
+		 * destination's runs */
+		constexpr int MT = mt_of<D, S>::v;
+		__shared__ __align__(16) S mtile[MT * (MT + 1)];
+		__shared__ __align__(16) D dtile[MT * MT];
 		__shared__ int64_t s_o[2][MAT_MAXQ];
 		const int s0 = (int)t.size[0], s1 = (int)t.size[1], n = s0 * s1;
 		const int ld = s0 + 1, pitch = s1 * ld;
@@ -214,6 +252,7 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		const int64_t o0 = local * m.rows_per_cta;
 		const int k = (int)(m.nouter - o0 < m.rows_per_cta ? m.nouter - o0 :
 		    m.rows_per_cta);
+		const bool rd = op != XMGD_OP_COPY;	/* the op reads dst */
 		for (int q = threadIdx.x; q < k; q += PT_THREADS)
 			outer_offsets(t, 2, o0 + q, s_o[0][q], s_o[1][q]);
 		__syncthreads();
@@ -221,14 +260,14 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		/* flattened walks with the mixed-radix digits advanced by the
 		 * thread stride (one division per CTA, not per element) */
 		{
-			/* loads: e = q n + i0 s1 + i1 (source runs along i1) */
+			/* source: e = q n + i0 s1 + i1 (runs along i1) */
 			int q = threadIdx.x / n, r = threadIdx.x - q * n;
 			int i0 = r / s1, i1 = r - i0 * s1;
 			const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
 			const int d0 = dr / s1, d1 = dr - d0 * s1;
-#pragma unroll 4
 			for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
-				mtile[q * pitch + i1 * ld + i0] = src[s_o[1][q] + i0 * ss0 + i1];
+				cp_async_elem(&mtile[q * pitch + i1 * ld + i0],
+				    &src[s_o[1][q] + i0 * ss0 + i1]);
 				i1 += d1;
 				if (i1 >= s1) { i1 -= s1; i0++; }
 				i0 += d0;
@@ -236,23 +275,35 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 				q += dq;
 			}
 		}
-		__syncthreads();
-		{
-			/* stores: e = q n + i1 s0 + i0 (destination runs along i0) */
-			int q = threadIdx.x / n, r = threadIdx.x - q * n;
-			int i1 = r / s0, i0 = r - i1 * s0;
-			const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
-			const int d1 = dr / s0, d0 = dr - d1 * s0;
-#pragma unroll 4
+		/* destination: e = q n + i1 s0 + i0 (runs along i0); tile slot e */
+		int q = threadIdx.x / n, r = threadIdx.x - q * n;
+		int i1 = r / s0, i0 = r - i1 * s0;
+		const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
+		const int d1 = dr / s0, d0 = dr - d1 * s0;
+		if (rd) {
+			int qq = q, j0 = i0, j1 = i1;
 			for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
-				elem_op<D, S>::apply(op, dst + s_o[0][q] + i0 + i1 * ds1,
-				    &mtile[q * pitch + i1 * ld + i0], al, als, be, dre, dim_);
-				i0 += d0;
-				if (i0 >= s0) { i0 -= s0; i1++; }
-				i1 += d1;
-				if (i1 >= s1) { i1 -= s1; q++; }
-				q += dq;
+				cp_async_elem(&dtile[e], dst + s_o[0][qq] + j0 + j1 * ds1);
+				j0 += d0;
+				if (j0 >= s0) { j0 -= s0; j1++; }
+				j1 += d1;
+				if (j1 >= s1) { j1 -= s1; qq++; }
+				qq += dq;
 			}
+		}
+		cp_async_wait_all();
+		__syncthreads();
+		for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
+			D v = rd ? dtile[e] : D();
+			elem_op<D, S>::apply(op, &v, &mtile[q * pitch + i1 * ld + i0], al,
+			    als, be, dre, dim_);
+			if (op != XMGD_OP_DOT)
+				dst[s_o[0][q] + i0 + i1 * ds1] = v;
+			i0 += d0;
+			if (i0 >= s0) { i0 -= s0; i1++; }
+			i1 += d1;
+			if (i1 >= s1) { i1 -= s1; q++; }
+			q += dq;
 		}
 	} else {
 		/* tile: dims 0 (dst unit stride) and 1 (src unit stride) */
@@ -346,13 +397,13 @@ elem_bytes(int type)
  * and the task copy follow the grouped order.
  */
 static void
-plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int stype,
+plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int dtype, int stype,
     std::vector<xmgd_ptask_t> &sorted, std::vector<task_meta> &meta,
     std::vector<int> &order, int64_t begin[5])
 {
 	std::vector<task_meta> m0((size_t)ntasks);
 	std::vector<int64_t> cnt((size_t)ntasks);
-	const int mt = elem_bytes(stype) <= 8 ? 64 : 32;
+	const int mt = mt_host(elem_bytes(dtype), elem_bytes(stype));
 
 	for (int i = 0; i < ntasks; i++) {
 		const xmgd_ptask_t &t = tasks[i];
@@ -470,7 +521,8 @@ xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, int stype,
 	memset(b, 0, sizeof *b);
 	if (ntasks <= 0)
 		return XMG_OK;
-	plan_tasks(tasks, ntasks, stype, sorted, meta, order, b->begin);
+	/* batches staged for replay carry one type on both sides */
+	plan_tasks(tasks, ntasks, stype, stype, sorted, meta, order, b->begin);
 	if ((st = xmgd_alloc(tb + meta.size() * sizeof(task_meta), &b->dbuf)))
 		return st;
 	b->ntasks = ntasks;
@@ -507,7 +559,7 @@ xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
 
 	if (ntasks <= 0)
 		return XMG_OK;
-	plan_tasks(tasks, ntasks, stype, sorted, meta, order, begin);
+	plan_tasks(tasks, ntasks, dtype, stype, sorted, meta, order, begin);
 	nctas = begin[4];
 	tb = task_bytes(ntasks);
 	mb = (size_t)ntasks * sizeof(task_meta);
