@@ -154,8 +154,32 @@ emu_exp_kernel(const xmgd_view_t *__restrict__ views,
 	const int k0 = kb * 256, k1 = min(kall, k0 + 256);
 	int bad = 0;
 
-	if (w.kfast) {
-		/* K contiguous: a warp walks K for one row at a time */
+	if (w.kcontig && !w.cplx) {
+		/* K one contiguous run per row: a warp walks it directly (no
+		 * offset table), four loads in flight per lane; the padding past
+		 * w.k is zero and needs no reading */
+		const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+		const T *base = X + rowt[0];
+		const int kend = min(k1, w.k);
+		for (int rr = warp; rr < EMU_TM; rr += 8) {
+			int r = rt * EMU_TM + rr;
+			if (r >= w.mn)
+				break;
+			const T *xr = base + colt[r];
+			int e = 0;
+#pragma unroll 4
+			for (int k = k0 + lane; k < kend; k += 32) {
+				int b = fin<T>::bexp(xr[k]);
+				bad |= b == fin<T>::EMAX;
+				e = max(e, b);
+			}
+			for (int off = 16; off > 0; off >>= 1)
+				e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
+			if (lane == 0 && e > 0)
+				atomicMax(&E[w.exptab + r], e);
+		}
+	} else if (w.kfast) {
+		/* K unit-stride: a warp walks K for one row at a time */
 		const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
 		for (int rr = warp; rr < EMU_TM; rr += 8) {
 			int r = rt * EMU_TM + rr;
@@ -1303,6 +1327,9 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 			w.khp = EMU_KS * ((w.k + EMU_KS - 1) / EMU_KS);
 			w.n_ks = (cplx ? 2 : 1) * (w.khp / EMU_KS);
 			w.kfast = w.k > 1 && p->tabs[w.rowtab + 1] - p->tabs[w.rowtab] == 1;
+			w.kcontig = w.kfast;
+			for (int32_t k = 2; w.kcontig && k < w.k; k++)
+				w.kcontig = p->tabs[w.rowtab + k] - p->tabs[w.rowtab] == k;
 			w.slices = off;
 			off += (size_t)w.n_rt * w.n_ks * chunk_bytes;
 		}

@@ -115,7 +115,8 @@ typedef struct {
 	int32_t kfast;               /* rows (K) unit-stride in memory */
 	int32_t cplx;                /* complex elements: realified K */
 	int32_t khp;                 /* complex: K per half, padded to 16 */
-	int32_t pad2;
+	int32_t kcontig;             /* rows (K) contiguous: row offset k is
+	                                row offset 0 + k for every k */
 	uint64_t slices;             /* device address of the tiled slices */
 } xmgd_view_t;
 
