@@ -230,7 +230,7 @@ __device__ __forceinline__ uint32_t digit_bf16(int d, float w)
 
 /* CTA = (view, 128-row tile, group of 4 K steps); thread = (row, K octet) */
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
 emu_split_kernel(const xmgd_view_t *__restrict__ views,
     const view_meta *__restrict__ meta, int nviews,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ E)
@@ -250,6 +250,9 @@ emu_split_kernel(const xmgd_view_t *__restrict__ views,
 	const int32_t co = live ? colt[r] : 0;
 	const int er = live ? E[w.exptab + r] : 0;
 	uint16_t *out = reinterpret_cast<uint16_t *>(w.slices);
+	/* a contiguous K run: direct loads, no offset table */
+	const bool direct = w.kcontig && !w.cplx;
+	const T *Xr = X + co + (direct ? rowt[0] : 0);
 
 	for (int ks = g * 4; ks < min(w.n_ks, g * 4 + 4); ks++) {
 		uint32_t bits[S][4];
@@ -261,7 +264,8 @@ emu_split_kernel(const xmgd_view_t *__restrict__ views,
 #pragma unroll
 		for (int e = 0; e < 8; e++) {
 			const int k = ks * EMU_KS + oct * 8 + e;
-			T x = live ? fetch(X, rowt, co, w, k) : T(0);
+			T x = !live ? T(0) : direct ? (k < w.k ? Xr[k] : T(0)) :
+			    fetch(X, rowt, co, w, k);
 			long long m;
 			int eb;
 			bool neg;
