@@ -25,6 +25,7 @@
  */
 #include <stdlib.h>
 #include <string.h>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -165,6 +166,72 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 		    FLAT_ELEMS);
 		D *dp = dst + base;
 		const S *sp = src + base;
+		bool done = false;
+		if constexpr (std::is_same<D, S>::value && sizeof(D) < 16) {
+			/* 16-byte accesses when both runs start on a 16-byte
+			 * boundary (whole blocks do), scalar tail */
+			constexpr int W = 16 / sizeof(D);
+			struct alignas(16) vec { D v[W]; };
+			const bool al16 = ((reinterpret_cast<uintptr_t>(dp) |
+			    reinterpret_cast<uintptr_t>(sp)) & 15) == 0;
+			const int nv = n / W;
+			vec *dv = reinterpret_cast<vec *>(dp);
+			const vec *sv = reinterpret_cast<const vec *>(sp);
+			done = al16;
+			if (al16) {
+				switch (op) {
+				case XMGD_OP_SET: {
+					vec a;
+#pragma unroll
+					for (int w = 0; w < W; w++)
+						a.v[w] = al;
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS)
+						dv[e] = a;
+					break;
+				}
+				case XMGD_OP_SCALE:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						vec x = dv[e];
+#pragma unroll
+						for (int w = 0; w < W; w++)
+							x.v[w] = num<D>::mul(al, x.v[w]);
+						dv[e] = x;
+					}
+					break;
+				case XMGD_OP_AXPY:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						vec x = dv[e];
+						const vec y = sv[e];
+#pragma unroll
+						for (int w = 0; w < W; w++)
+							x.v[w] = num<D>::add(num<D>::mul(al, x.v[w]),
+							    num<D>::mul(be, y.v[w]));
+						dv[e] = x;
+					}
+					break;
+				case XMGD_OP_COPY:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						const vec y = sv[e];
+						vec x;
+#pragma unroll
+						for (int w = 0; w < W; w++)
+							x.v[w] = num<D>::mul(als, y.v[w]);
+						dv[e] = x;
+					}
+					break;
+				default:
+					done = false;
+				}
+			}
+			if (done)
+				for (int e = nv * W + threadIdx.x; e < n; e += PT_THREADS)
+					elem_op<D, S>::apply(op, dp + e, sp + e, al, als, be, dre, dim_);
+		}
+		if (!done)
 		switch (op) {
 		case XMGD_OP_SET:
 #pragma unroll 4
