@@ -7,7 +7,7 @@ Workload: the uneven-block, Z2^3-sparse FP64 ladder
     C(i,j,a,b) = sum_{c,d} A(i,j,c,d) B(c,d,a,b)
 o = 96 in 6 blocks of 8..24, v = 384 in 12 blocks of 16..48, i<->j, c<->d,
 a<->b antisymmetry, seeded uniform[-1,1] data (synthetic: splitmix64).
-Inputs (A ~0.3 GB, B ~5.4 GB) are larger than L2, so no flush is needed.
+Inputs (A ~0.3 GB, B ~7.8 GB) are larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
