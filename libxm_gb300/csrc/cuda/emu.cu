@@ -96,13 +96,23 @@ template <> struct fin<float> {
 	{ return (int)((__float_as_uint(x) >> 23) & 0xff); }
 };
 
-/* one output tile: block, row offsets in b's (j0) and a's (i0) view, and
- * pr = pass (bit 0) | swap (bit 1) | live N-side rows << 8 (a multiple of
- * 16).  Without swap b's view is the 128-row M side (TMEM lanes) and a's
- * the N side (TMEM columns); swap exchanges them. */
+/* One work item: a 128-row tile of the M-side view (rows m0 ..) against
+ * the N-side tiles of up to EMU_MAXMEM output blocks stacked along N
+ * (members mfirst .. mfirst + mcount - 1); pr = pass (bit 0) | swap (bit
+ * 1) | live N rows in all << 8 (a multiple of 16).  Without swap b's view
+ * is the 128-row M side (TMEM lanes) and a's the N side (TMEM columns);
+ * swap exchanges them.  The members of an item share the M side: for
+ * every pair index the same M-side view and K. */
 struct emu_item {
-	int32_t cblock, j0, i0, pr;
+	int32_t m0, mfirst, mcount, pr;
 };
+
+/* a member: output block, first N-side row of its tile in that block's
+ * N-side view, live rows (a multiple of 16), first TMEM column */
+struct emu_member {
+	int32_t cblock, n0, rows, off;
+};
+constexpr int EMU_MAXMEM = 4;
 
 struct view_meta {
 	int64_t first_cta;
@@ -406,6 +416,7 @@ issue_step(uint32_t tmem, uint32_t base, uint32_t a_off, uint32_t idesc,
 template <int S, int KEEP, bool LOW, typename TOUT, int DW, bool PAIR>
 __global__ void __launch_bounds__(64 + 32 * DW, 1)
 emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
+    const emu_member *__restrict__ members,
     const xmgd_cblock_t *__restrict__ cbs, const xmgd_pair_t *__restrict__ prs,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ EA,
@@ -532,24 +543,42 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				if (t < 0)
 					break;
 				const emu_item it = items[t];
-				const xmgd_cblock_t cb = cbs[it.cblock];
+				const int nmem = it.mcount;
+				const xmgd_cblock_t cb = cbs[members[it.mfirst].cblock];
 				const int pass = it.pr & 1, swp = (it.pr >> 1) & 1;
 				/* M side: 128 rows (this CTA's half of 256 in a pair);
-				 * N side: the live rows only (a pair: this CTA's half) */
-				const uint32_t nbytes = (uint32_t)(it.pr >> 8) * S * 32 / (PAIR ? 2 : 1);
-				const uint32_t noff = PAIR ? rank * nbytes : 0;
+				 * N side: every member's live rows at its first column
+				 * (a pair: one member, this CTA's half of its rows) */
+				const uint32_t ntot = (uint32_t)(it.pr >> 8) * S * 32 / (PAIR ? 2 : 1);
+				const uint32_t noff = PAIR ? rank * ntot : 0;
+				int mfp[EMU_MAXMEM], mrt[EMU_MAXMEM];
+				uint32_t mby[EMU_MAXMEM], mdo[EMU_MAXMEM];
+#pragma unroll
+				for (int j = 0; j < EMU_MAXMEM; j++) {
+					const emu_member mb = members[it.mfirst + (j < nmem ? j : 0)];
+					mfp[j] = cbs[mb.cblock].first_pair;
+					mrt[j] = mb.n0 / EMU_TM;
+					mby[j] = PAIR ? ntot : (uint32_t)mb.rows * S * 32;
+					mdo[j] = (uint32_t)mb.off * S * 32;
+				}
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
+					/* the members' pair lists run in step: pair p of every
+					 * member has member 0's M-side view and K */
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
-					const xmgd_view_t wb = vb[pr.bview], wa = va[pr.aview];
-					const int nks = wb.n_ks, nh = nks / 2;
-					const int mtile = (swp ? it.i0 : it.j0) / EMU_TM + (int)rank;
-					const int ntile = (swp ? it.j0 : it.i0) / EMU_TM;
-					const bool mlive = mtile < (swp ? wa.n_rt : wb.n_rt);
-					const uint8_t *gm = reinterpret_cast<const uint8_t *>(
-					    swp ? wa.slices : wb.slices) + (size_t)mtile * nks * C::CHUNK_BYTES;
-					const uint8_t *gn = reinterpret_cast<const uint8_t *>(
-					    swp ? wb.slices : wa.slices) + (size_t)ntile * nks * C::CHUNK_BYTES +
-					    noff;
+					const xmgd_view_t wm = swp ? va[pr.aview] : vb[pr.bview];
+					const int nks = vb[pr.bview].n_ks, nh = nks / 2;
+					const int mtile = it.m0 / EMU_TM + (int)rank;
+					const bool mlive = mtile < wm.n_rt;
+					const uint8_t *gm = reinterpret_cast<const uint8_t *>(wm.slices) +
+					    (size_t)mtile * nks * C::CHUNK_BYTES;
+					const uint8_t *gn[EMU_MAXMEM];
+#pragma unroll
+					for (int j = 0; j < EMU_MAXMEM; j++) {
+						const xmgd_pair_t pj = prs[mfp[j] + p];
+						gn[j] = reinterpret_cast<const uint8_t *>(swp ?
+						    vb[pj.bview].slices : va[pj.aview].slices) +
+						    (size_t)mrt[j] * nks * C::CHUNK_BYTES + noff;
+					}
 					for (int ks = 0; ks < nks; ks++) {
 						if (!wait(smem_u32(&bar_empty[s]), ph ^ 1, 1))
 							break;
@@ -560,12 +589,15 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						uint32_t fb = smem_u32(&bar_full[s]);
 						/* a pair's second M tile may lie past the view: its
 						 * rows are then never stored */
-						mbar_expect_tx(fb, (mlive ? C::CHUNK_BYTES : 0) + nbytes);
+						mbar_expect_tx(fb, (mlive ? C::CHUNK_BYTES : 0) + ntot);
 						if (mlive)
 							bulk_g2s(dst, gm + (size_t)km * C::CHUNK_BYTES,
 							    C::CHUNK_BYTES, fb);
-						bulk_g2s(dst + C::CHUNK_BYTES, gn + (size_t)kn * C::CHUNK_BYTES,
-						    nbytes, fb);
+#pragma unroll
+						for (int j = 0; j < EMU_MAXMEM; j++)
+							if (j < nmem)
+								bulk_g2s(dst + C::CHUNK_BYTES + mdo[j],
+								    gn[j] + (size_t)kn * C::CHUNK_BYTES, mby[j], fb);
 #pragma unroll
 						for (int q = 0; q < NST; q++)
 							if (q == s)
@@ -600,7 +632,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				if (++slot == 2) { slot = 0; iph ^= 1; }
 				if (t < 0)
 					break;
-				const xmgd_cblock_t cb = cbs[items[t].cblock];
+				const xmgd_cblock_t cb = cbs[members[items[t].mfirst].cblock];
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					const int nks = vb[prs[cb.first_pair + p].bview].n_ks;
 					for (int ks = 0; ks < nks; ks++) {
@@ -642,7 +674,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				if (t < 0)
 					break;
 				const emu_item it = items[t];
-				const xmgd_cblock_t cb = cbs[it.cblock];
+				const xmgd_cblock_t cb = cbs[members[it.mfirst].cblock];
 				const uint32_t idesc = PAIR ? idesc_pair_n(it.pr >> 8) : idesc_n(it.pr >> 8);
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
@@ -761,6 +793,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 		 * warp w reads TMEM lanes 32 * (w % 4) .. +31 (the tcgen05.ld
 		 * lane-quadrant rule) and owns NC of the 128 columns */
 		constexpr int NC = 128 / (DW / 4);
+		constexpr int NSEG = NC / 16;
 		const int quad = warp & 3, half = (warp - 2) >> 2;
 		const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + half * NC;
 		uint32_t fph = 0;
@@ -780,26 +813,50 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			if (t < 0)
 				break;
 			const emu_item it = items[t];
-			const xmgd_cblock_t cb = cbs[it.cblock];
-			const int F = cbF[it.cblock];
 			const int pass = it.pr & 1, swp = (it.pr >> 1) & 1, rows = it.pr >> 8;
+			/* this warp's NC columns fall into NC / 16 segments of 16, each
+			 * inside one member (members hold multiples of 16 rows): per
+			 * segment the output block, its first pair, its F and the
+			 * N-side row of the segment's first column */
+			int scb[NSEG], sfp[NSEG], sF[NSEG], sq0[NSEG];
+#pragma unroll
+			for (int g = 0; g < NSEG; g++) {
+				const int col = half * NC + g * 16;
+				int j = 0;
+				for (int jj = 1; jj < it.mcount; jj++)
+					j += col >= members[it.mfirst + jj].off;
+				const emu_member mb = members[it.mfirst + j];
+				scb[g] = mb.cblock;
+				sfp[g] = cbs[mb.cblock].first_pair;
+				sF[g] = cbF[mb.cblock];
+				sq0[g] = mb.n0 + col - mb.off;
+			}
+			const int npairs = cbs[scb[0]].npairs;
 			long long V[NC];
 #pragma unroll
 			for (int c = 0; c < NC; c++)
 				V[c] = 0;
-			for (int p = 0; p < cb.npairs && ok; p++) {
-				const xmgd_pair_t pr = prs[cb.first_pair + p];
-				const int nks = vb[pr.bview].n_ks;
+			for (int p = 0; p < npairs && ok; p++) {
+				const int nks = vb[prs[sfp[0] + p].bview].n_ks;
+				int esg[NSEG], esh[NSEG];
+#pragma unroll
+				for (int g = 0; g < NSEG; g++) {
+					const xmgd_pair_t pg = prs[sfp[g] + p];
+					esg[g] = pg.esign;
+					esh[g] = pg.eshift;
+				}
 				for (int c0 = 0; c0 < nks; ) {
 					const int c1 = chunk_end(c0, nks, cplx);
-					/* the pair factor sign * 2^shift (shift 0 or 1, checked
-					 * by the planner) rides on the exact fp32 -> int
-					 * scales; the real pass negates the im * im half */
+					/* each segment's pair factor sign * 2^shift (shift 0
+					 * or 1, checked by the planner) rides on the exact
+					 * fp32 -> int scales; the real pass negates the im * im
+					 * half */
 					const bool negh = cplx && !pass && c0 >= nks / 2;
-					const float sg = (pr.esign > 0) != negh ? 1.0f : -1.0f;
-					const float s0 = sg * __int_as_float((127 + pr.eshift) << 23);
-					const float s1 = s0 * 256.0f, s2 = s0 * 65536.0f;
-					const float s3 = s0 * __int_as_float((127 + 16 + F) << 23);
+					float s0[NSEG];
+#pragma unroll
+					for (int g = 0; g < NSEG; g++)
+						s0[g] = ((esg[g] > 0) != negh ? 1.0f : -1.0f) *
+						    __int_as_float((127 + esh[g]) << 23);
 					/* one lane waits, the warp follows its verdict, so the
 					 * .sync.aligned TMEM loads below stay convergent */
 					int w = 1;
@@ -818,6 +875,9 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					for (int b4 = 0; b4 < NC / 4; b4++) {
 						if (half * NC + b4 * 4 >= rows)
 							break;	/* warp-uniform: columns past the tile */
+						const int g = b4 / 4, F = sF[g];
+						const float s2 = s0[g] * 65536.0f;
+						const float s3 = s0[g] * __int_as_float((127 + 16 + F) << 23);
 						float ax[4];
 						tmem_ld4(trow + XACC * 128 + b4 * 4, ax);
 						tmem_wait_ld();
@@ -858,6 +918,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					for (int b4 = 0; b4 < NC / 4; b4++) {
 						if (half * NC + b4 * 4 >= rows)
 							break;
+						const int g = b4 / 4, F = sF[g];
+						const float sa = s0[g], sb = sa * 256.0f, sc = sa * 65536.0f;
 						float a0[4], a1[4], a2[4];
 						tmem_ld4(trow + 0 * 128 + b4 * 4, a0);
 						tmem_ld4(trow + 1 * 128 + b4 * 4, a1);
@@ -868,11 +930,11 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						for (int c = 0; c < 4; c++) {
 							/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
 							 * |i0 * 256 + i1| < 2^31 */
-							int i0 = __float2int_rn(a0[c] * s0);
-							int i1 = __float2int_rn(a1[c] * s1);
+							int i0 = __float2int_rn(a0[c] * sa);
+							int i1 = __float2int_rn(a1[c] * sb);
 							long long d = (long long)(i0 * 256 + i1) << 8;
 							if (LOW)
-								d += __float2int_rn(a2[c] * s2);
+								d += __float2int_rn(a2[c] * sc);
 							V[b4 * 4 + c] += d << F;
 						}
 					}
@@ -887,35 +949,39 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				break;
 			/* epilogue (overlaps the next item's first chunk of MMAs):
 			 * this thread's TMEM lane is one M-side row; its columns are
-			 * N-side rows.  Without swap the M side is b's free index (j),
-			 * with swap a's (i). */
-			const int ms = (swp ? it.i0 : it.j0) + (int)rank * EMU_TM + quad * 32 + lane;
-			const int q0 = (swp ? it.j0 : it.i0) + half * NC;
-			const int flim = swp ? cb.m : cb.n, vlim = swp ? cb.n : cb.m;
-			if (ms < flim) {
+			 * N-side rows of the segments' output blocks.  Without swap
+			 * the M side is b's free index (j), with swap a's (i). */
+			const int ms = it.m0 + (int)rank * EMU_TM + quad * 32 + lane;
+			const bool bz = beta == 0.0;
+			const int cm = cplx ? 2 : 1;
+			/* alpha a normal power of two folds into the exponent and
+			 * sign; any other alpha costs one multiply */
+			const long long ab = __double_as_longlong(alpha);
+			const int aex = (int)((ab >> 52) & 0x7ff);
+			const bool apow2 = (ab & 0xFFFFFFFFFFFFFll) == 0 && aex > 0 && aex < 0x7ff;
+			const int esa = apow2 ? aex - 1023 : 0;
+			const unsigned long long asx = apow2 ?
+			    (unsigned long long)ab & (1ull << 63) : 0ull;
+#pragma unroll
+			for (int g = 0; g < NSEG; g++) {
+				const xmgd_cblock_t cb = cbs[scb[g]];
+				const int flim = swp ? cb.m : cb.n, vlim = swp ? cb.n : cb.m;
+				if (ms >= flim)
+					continue;
 				TOUT *Cp = reinterpret_cast<TOUT *>(cb.c_ptr);
 				const int32_t *vtab = tabs + (swp ? cb.ccol : cb.crow);
 				const int32_t *vexp = swp ? EB + cb.eB : EA + cb.eA;
 				const int32_t fo = tabs[(swp ? cb.crow : cb.ccol) + ms];
 				const int fe = (swp ? EA + cb.eA : EB + cb.eB)[ms];
-				const bool bz = beta == 0.0;
-				const int cm = cplx ? 2 : 1;
-				/* alpha a normal power of two folds into the exponent
-				 * and sign; any other alpha costs one multiply */
-				const long long ab = __double_as_longlong(alpha);
-				const int aex = (int)((ab >> 52) & 0x7ff);
-				const bool apow2 = (ab & 0xFFFFFFFFFFFFFll) == 0 && aex > 0 && aex < 0x7ff;
-				const int esh = apow2 ? aex - 1023 : 0;
-				const unsigned long long asx = apow2 ?
-				    (unsigned long long)ab & (1ull << 63) : 0ull;
+				const int F = sF[g];
 #pragma unroll
-				for (int c = 0; c < NC; c++) {
-					const int q = q0 + c;
-					if (q < vlim) {
+				for (int c = 0; c < 16; c++) {
+					const int q = sq0[g] + c;
+					if (q < vlim && half * NC + g * 16 + c < rows) {
 						const int e = vexp[q] + fe - expoff2 - 16 - F;
 						double v;
-						if (!pack_f64(V[c], e + esh, asx, v))
-							v = alpha * ldexp((double)V[c], e);
+						if (!pack_f64(V[g * 16 + c], e + esa, asx, v))
+							v = alpha * ldexp((double)V[g * 16 + c], e);
 						else if (!apow2)
 							v *= alpha;
 						TOUT *cp = Cp + (size_t)cm * (vtab[q] + fo) + pass;
@@ -971,6 +1037,18 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
  */
 enum { EMU_NPOLICY = 3 };
 
+/* policy 6: policy 2's orientation and order, with the N-side tails of the
+ * output blocks that share an M side (the same M-side view and K for every
+ * pair index) stacked into common 128-column tiles: the MMAs of a K step
+ * get wider, the shared-memory operand reads per flop fewer */
+enum { EMU_POL_MERGED = 2 * EMU_NPOLICY };
+
+static bool
+pair_policy(int pol)
+{
+	return pol >= EMU_NPOLICY && pol < 2 * EMU_NPOLICY;
+}
+
 /* CTA pairs (256-row M tiles, cta_group::2): policies 3..5 repeat 0..2 in
  * that form; offered to the tuner when XMG_CTA_PAIR=1 */
 static bool
@@ -1008,7 +1086,7 @@ static std::vector<tune_entry> g_tuned;
 
 struct emu_cand {
 	int policy;
-	uint64_t d_items;
+	uint64_t d_items, d_members;
 	int nitems, grid;
 	float ms;
 };
@@ -1083,7 +1161,7 @@ launch_gemm(emu_plan *e)
 	int32_t *EA = (int32_t *)e->d_E, *EB = EA + e->nexp_a;
 	int *flags = (int *)(EA + e->nE);
 
-	if (c.policy >= EMU_NPOLICY) {
+	if (pair_policy(c.policy)) {
 		/* clusters of two CTAs */
 		cudaLaunchConfig_t cfg = {};
 		cudaLaunchAttribute at[1];
@@ -1098,14 +1176,16 @@ launch_gemm(emu_plan *e)
 		cfg.attrs = at;
 		cfg.numAttrs = 1;
 		XMG_CK(cudaLaunchKernelEx(&cfg, emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, true>,
-		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
+		    (const emu_item *)c.d_items, c.nitems, (const emu_member *)c.d_members,
+		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    (const int32_t *)EA, (const int32_t *)EB, (const int32_t *)e->d_F,
 		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags));
 	} else {
 		emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, false><<<(unsigned)c.grid,
 		    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
-		    (const emu_item *)c.d_items, c.nitems, e->d_cbs, e->d_prs,
+		    (const emu_item *)c.d_items, c.nitems, (const emu_member *)c.d_members,
+		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
 		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags);
@@ -1156,9 +1236,12 @@ emu_free(emu_plan *e)
 	for (uint64_t b : bufs)
 		if (b)
 			xmgd_free(b);
-	for (emu_cand &c : e->cand)
+	for (emu_cand &c : e->cand) {
 		if (c.d_items)
 			xmgd_free(c.d_items);
+		if (c.d_members)
+			xmgd_free(c.d_members);
+	}
 	if (e->h_flags)
 		cudaFreeHost(e->h_flags);
 	delete e;
@@ -1167,15 +1250,16 @@ emu_free(emu_plan *e)
 /* work list of one policy (see above) */
 static void
 make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
-    int policy, std::vector<emu_item> &items)
+    int policy, std::vector<emu_item> &items, std::vector<emu_member> &members)
 {
 	struct blk {
 		int ci, swp, mlen, nlen;
 		double cost;
 		uint64_t key;
 	};
-	const int base = policy % EMU_NPOLICY;
-	const int mstep = policy >= EMU_NPOLICY ? 2 * EMU_TM : EMU_TM;
+	const bool merged = policy == EMU_POL_MERGED;
+	const int base = merged ? 2 : policy % EMU_NPOLICY;
+	const int mstep = pair_policy(policy) ? 2 * EMU_TM : EMU_TM;
 	const int pol = base == 2 ? 2 : 0;
 	std::vector<blk> bl;
 	for (int ci : cblocks) {
@@ -1193,16 +1277,25 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 		b.key = ((uint64_t)b.swp << 40) | (uint32_t)(b.swp ? cb.eA : cb.eB);
 		bl.push_back(b);
 	}
+	/* one item per member list (every complex pass) */
+	auto push = [&](int m0, int swp, const std::vector<emu_member> &mem) {
+		int tot = 0;
+		for (const emu_member &x : mem)
+			tot += x.rows;
+		for (int ps = 0; ps < (cplx ? 2 : 1); ps++) {
+			items.push_back(emu_item{m0, (int)members.size(), (int)mem.size(),
+			    ps | (swp ? 2 : 0) | (tot << 8)});
+			members.insert(members.end(), mem.begin(), mem.end());
+		}
+	};
 	auto emit = [&](const blk &b, int m0) {
 		for (int n0 = 0; n0 < b.nlen; n0 += EMU_TM) {
 			const int rows = std::min(EMU_TM, (b.nlen - n0 + 15) / 16 * 16);
-			const int i0 = b.swp ? m0 : n0, j0 = b.swp ? n0 : m0;
-			for (int ps = 0; ps < (cplx ? 2 : 1); ps++)
-				items.push_back(emu_item{b.ci, j0, i0,
-				    ps | (b.swp ? 2 : 0) | (rows << 8)});
+			push(m0, b.swp, {emu_member{b.ci, n0, rows, 0}});
 		}
 	};
 	items.clear();
+	members.clear();
 	std::stable_sort(bl.begin(), bl.end(),
 	    [](const blk &x, const blk &y) { return x.cost > y.cost; });
 	if (base == 0) {
@@ -1212,18 +1305,32 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 		return;
 	}
 	/* grouped: blocks reading the same M-side rows together, M tile by
-	 * M tile, groups by decreasing cost */
-	std::vector<std::pair<uint64_t, std::vector<int>>> groups;
+	 * M tile, groups by decreasing cost; merged: a group holds only
+	 * blocks whose pair lists have the same M-side view and K at every
+	 * index, so their tiles can share the M-side stages */
+	std::vector<std::vector<int64_t>> gkey;
+	std::vector<std::vector<int>> groups;
 	std::vector<double> gcost;
+	std::vector<int64_t> k;
 	for (int i = 0; i < (int)bl.size(); i++) {
+		k.assign(1, (int64_t)bl[i].key);
+		if (merged) {
+			const xmgd_cblock_t &cb = p->cblocks[bl[i].ci];
+			k.push_back(bl[i].mlen);
+			for (int q = 0; q < cb.npairs; q++) {
+				const xmgd_pair_t &pr = p->pairs[cb.first_pair + q];
+				k.push_back(((int64_t)(bl[i].swp ? pr.aview : pr.bview) << 32) | pr.k);
+			}
+		}
 		size_t g = 0;
-		while (g < groups.size() && groups[g].first != bl[i].key)
+		while (g < groups.size() && gkey[g] != k)
 			g++;
 		if (g == groups.size()) {
-			groups.push_back({bl[i].key, {}});
+			gkey.push_back(k);
+			groups.push_back({});
 			gcost.push_back(0);
 		}
-		groups[g].second.push_back(i);
+		groups[g].push_back(i);
 		gcost[g] += bl[i].cost;
 	}
 	std::vector<int> go(groups.size());
@@ -1233,13 +1340,94 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 	    [&](int x, int y) { return gcost[x] > gcost[y]; });
 	for (int g : go) {
 		int mmax = 0;
-		for (int i : groups[g].second)
+		for (int i : groups[g])
 			mmax = std::max(mmax, bl[i].mlen);
-		for (int m0 = 0; m0 < mmax; m0 += mstep)
-			for (int i : groups[g].second)
-				if (m0 < bl[i].mlen)
-					emit(bl[i], m0);
+		for (int m0 = 0; m0 < mmax; m0 += mstep) {
+			if (!merged) {
+				for (int i : groups[g])
+					if (m0 < bl[i].mlen)
+						emit(bl[i], m0);
+				continue;
+			}
+			/* full 128-row N tiles alone; the partial ones packed
+			 * first-fit decreasing into tiles of <= 128 rows and
+			 * <= EMU_MAXMEM members */
+			std::vector<emu_member> part;
+			for (int i : groups[g]) {
+				const blk &b = bl[i];
+				for (int n0 = 0; n0 < b.nlen; n0 += EMU_TM) {
+					const int rows = std::min(EMU_TM, (b.nlen - n0 + 15) / 16 * 16);
+					if (rows == EMU_TM)
+						push(m0, b.swp, {emu_member{b.ci, n0, rows, 0}});
+					else
+						part.push_back(emu_member{b.ci, n0, rows, 0});
+				}
+			}
+			std::stable_sort(part.begin(), part.end(),
+			    [](const emu_member &x, const emu_member &y) { return x.rows > y.rows; });
+			std::vector<std::vector<emu_member>> bins;
+			std::vector<int> fill;
+			for (const emu_member &x : part) {
+				size_t b = 0;
+				while (b < bins.size() && (fill[b] + x.rows > EMU_TM ||
+				    (int)bins[b].size() == EMU_MAXMEM))
+					b++;
+				if (b == bins.size()) {
+					bins.push_back({});
+					fill.push_back(0);
+				}
+				emu_member y = x;
+				y.off = fill[b];
+				bins[b].push_back(y);
+				fill[b] += x.rows;
+			}
+			for (const auto &mem : bins)
+				push(m0, bl[groups[g][0]].swp, mem);
+		}
 	}
+}
+
+/* The invariants the kernel's addressing relies on, checked on the host
+ * before a work list is uploaded: member tiles inside their views and the
+ * stage (rows multiples of 16, stacked without gaps, <= 128 in all), and
+ * members that share the M side pair by pair. */
+static bool
+items_ok(const xmgd_contract_t *p, const std::vector<emu_item> &items,
+    const std::vector<emu_member> &mem, bool pair)
+{
+	for (const emu_item &it : items) {
+		if (it.mcount < 1 || it.mcount > (pair ? 1 : EMU_MAXMEM) || it.mfirst < 0 ||
+		    (size_t)it.mfirst + it.mcount > mem.size())
+			return false;
+		const int swp = (it.pr >> 1) & 1, tot = it.pr >> 8;
+		const xmgd_cblock_t &c0 = p->cblocks[mem[it.mfirst].cblock];
+		const int mlen = swp ? c0.m : c0.n;
+		if (it.m0 < 0 || it.m0 % EMU_TM || it.m0 >= mlen)
+			return false;
+		int off = 0;
+		for (int j = 0; j < it.mcount; j++) {
+			const emu_member &m = mem[it.mfirst + j];
+			if (m.cblock < 0 || m.cblock >= p->ncblocks)
+				return false;
+			const xmgd_cblock_t &cb = p->cblocks[m.cblock];
+			const int nlen = swp ? cb.n : cb.m;
+			if ((swp ? cb.m : cb.n) != mlen || cb.npairs != c0.npairs ||
+			    m.off != off || m.rows < 16 || m.rows % 16 || m.n0 < 0 ||
+			    m.n0 % EMU_TM || m.n0 >= nlen ||
+			    m.rows > std::min(EMU_TM, (nlen - m.n0 + 15) / 16 * 16))
+				return false;
+			for (int q = 0; q < cb.npairs; q++) {
+				const xmgd_pair_t &a = p->pairs[c0.first_pair + q];
+				const xmgd_pair_t &b = p->pairs[cb.first_pair + q];
+				if (a.k != b.k || (swp ? a.aview != b.aview : a.bview != b.bview))
+					return false;
+			}
+			off += m.rows;
+		}
+		if (off != tot || tot < 16 || tot > EMU_TM)
+			return false;
+	}
+	return true;
 }
 
 int
@@ -1382,29 +1570,45 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		known = 0;
 	if (getenv("XMG_POLICY"))	/* one fixed work-list policy */
 		known = atoi(getenv("XMG_POLICY"));
+	std::vector<int> pols = {0, 1, 2, EMU_POL_MERGED};
+	if (pairs_enabled())
+		pols.insert(pols.end(), {EMU_NPOLICY, EMU_NPOLICY + 1, EMU_NPOLICY + 2});
 	std::vector<std::vector<emu_item>> lists;
-	for (int pol = 0; pol < (pairs_enabled() ? 2 : 1) * EMU_NPOLICY; pol++) {
+	std::vector<std::vector<emu_member>> mlists;
+	for (int pol : pols) {
 		if (known >= 0 && pol != known)
 			continue;
 		std::vector<emu_item> items;
-		make_items(p, cblocks, cplx, pol, items);
+		std::vector<emu_member> mem;
+		make_items(p, cblocks, cplx, pol, items, mem);
+		if (!items_ok(p, items, mem, pair_policy(pol))) {
+			st = xmg_seterr(XMG_EINVAL, "split-precision path: work list %d "
+			    "failed its checks", pol);
+			goto fail;
+		}
 		bool dup = false;
-		for (auto &l : lists)
-			dup |= l.size() == items.size() && memcmp(l.data(), items.data(),
-			    items.size() * sizeof(emu_item)) == 0;
+		for (size_t l = 0; l < lists.size(); l++)
+			dup |= lists[l].size() == items.size() && mlists[l].size() == mem.size() &&
+			    memcmp(lists[l].data(), items.data(), items.size() * sizeof(emu_item)) == 0 &&
+			    memcmp(mlists[l].data(), mem.data(), mem.size() * sizeof(emu_member)) == 0;
 		if (dup)
 			continue;
 		emu_cand c;
 		c.policy = pol;
 		c.nitems = (int)items.size();
-		c.grid = pol >= EMU_NPOLICY ? 2 * std::min(c.nitems, num_sms() / 2) :
+		c.grid = pair_policy(pol) ? 2 * std::min(c.nitems, num_sms() / 2) :
 		    std::min(c.nitems, num_sms());
 		c.ms = -1;
+		c.d_items = c.d_members = 0;
 		if ((st = upload_new(items.data(), items.size() * sizeof(emu_item),
-		    &c.d_items)))
+		    &c.d_items)) || (st = upload_new(mem.data(), mem.size() *
+		    sizeof(emu_member), &c.d_members))) {
+			e->cand.push_back(c);	/* freed with the plan */
 			goto fail;
+		}
 		e->cand.push_back(c);
 		lists.push_back(std::move(items));
+		mlists.push_back(std::move(mem));
 	}
 	e->tuned = e->cand.size() <= 1;
 	if ((st = check(cudaMallocHost(&e->h_flags, 2 * sizeof(int)), "flags")) ||
