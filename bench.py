@@ -233,7 +233,7 @@ def block_costs(w):
 GEMM_DRAM_BYTES = 140.78e9 + 0.70118e9
 
 
-def timed_calls(eng, fn, reps=3, warm=3):
+def timed_calls(eng, fn, reps=3, warm=5):
     """Device time per call of fn after `warm` untimed calls (plan, tuning)."""
     for _ in range(warm):
         fn()
@@ -404,6 +404,11 @@ def engine_arm(args, ranks):
 
     def timed(prec, steps, warmup):
         eng.check(eng.xmg_set_precision(prec))
+        if prec != api.PREC_FP64:
+            # plan building and autotuning: the first calls of a new plan
+            # try each work-list candidate once (five at most)
+            for _ in range(5):
+                w.run()
         for _ in range(warmup):
             w.run()
         ranks.barrier()

@@ -1031,9 +1031,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
  *      max(N / 2, 32 + N / 4) cycles: the M-side operand (4 KiB) and the
  *      N-side operand (N * 32 B) are read from shared memory at 128 B per
  *      cycle while the tensor core needs N / 2 cycles.
- * The first runs of a plan replay each distinct policy once, timed with
- * events, then keep the fastest; the choice is remembered per block-size
- * histogram so later plans of the same shape start tuned.
+ * (and 6, the stacked form below, which runs first).  The first runs of a
+ * plan replay each distinct policy once, timed with events, then keep the
+ * fastest; the choice is remembered per block-size histogram so later
+ * plans of the same shape start tuned.
  */
 enum { EMU_NPOLICY = 3 };
 
@@ -1567,10 +1568,12 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		if (t.sig == sig)
 			known = t.policy;
 	if (getenv("XMG_TUNE") && strcmp(getenv("XMG_TUNE"), "0") == 0)
-		known = 0;
+		known = EMU_POL_MERGED;
 	if (getenv("XMG_POLICY"))	/* one fixed work-list policy */
 		known = atoi(getenv("XMG_POLICY"));
-	std::vector<int> pols = {0, 1, 2, EMU_POL_MERGED};
+	/* the stacked list first: a plan that runs once (an out-of-core
+	 * batch) never finishes tuning and keeps its first candidate */
+	std::vector<int> pols = {EMU_POL_MERGED, 0, 1, 2};
 	if (pairs_enabled())
 		pols.insert(pols.end(), {EMU_NPOLICY, EMU_NPOLICY + 1, EMU_NPOLICY + 2});
 	std::vector<std::vector<emu_item>> lists;
