@@ -96,19 +96,26 @@ template <> struct fin<float> {
 	{ return (int)((__float_as_uint(x) >> 23) & 0xff); }
 };
 
-/* One work item: a 128-row tile of the M-side view (rows m0 ..) against
- * the N-side tiles of up to EMU_MAXMEM output blocks stacked along N
- * (members mfirst .. mfirst + mcount - 1); pr = pass (bit 0) | swap (bit
- * 1) | live N rows in all << 8 (a multiple of 16).  Without swap b's view
- * is the 128-row M side (TMEM lanes) and a's the N side (TMEM columns);
- * swap exchanges them.  The members of an item share the M side: for
- * every pair index the same M-side view and K. */
+/* One work item: up to EMU_MAXMEM output blocks (members mfirst ..
+ * mfirst + mcount - 1) stacked along one side of a 128 x N tile that share
+ * the other side; pr = pass (bit 0) | swap (bit 1) | M-stacked (bit 2) |
+ * live N rows in all << 8 (a multiple of 16).  Without swap b's view is
+ * the M side (TMEM lanes) and a's the N side (TMEM columns); swap
+ * exchanges them.
+ *   N-stacked: m0 is the shared M-side tile (rows m0 .. m0 + 127 of the
+ *     M-side view); each member is an N-side tile of its block at TMEM
+ *     columns off .. off + rows - 1 (rows a multiple of 16).
+ *   M-stacked: m0 is the shared N-side tile; each member is an M-side
+ *     tile of its block at TMEM lanes off .. off + rows - 1 (off and rows
+ *     multiples of 32, so a drain warp's lanes lie in one member).
+ * Members share the other side pair by pair: the same view and K at every
+ * pair index. */
 struct emu_item {
 	int32_t m0, mfirst, mcount, pr;
 };
 
-/* a member: output block, first N-side row of its tile in that block's
- * N-side view, live rows (a multiple of 16), first TMEM column */
+/* a member: output block, first row of its tile in that block's view on
+ * the stacked side, live rows (rounded up), first TMEM column or lane */
 struct emu_member {
 	int32_t cblock, n0, rows, off;
 };
@@ -546,36 +553,42 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				const int nmem = it.mcount;
 				const xmgd_cblock_t cb = cbs[members[it.mfirst].cblock];
 				const int pass = it.pr & 1, swp = (it.pr >> 1) & 1;
-				/* M side: 128 rows (this CTA's half of 256 in a pair);
-				 * N side: every member's live rows at its first column
-				 * (a pair: one member, this CTA's half of its rows) */
+				const int mstk = (it.pr >> 2) & 1;
+				/* the shared side: the M side's 128 rows (this CTA's half
+				 * of 256 in a pair) or, M-stacked, the N side's live rows;
+				 * the members: their live rows at their first column or
+				 * lane (a pair: one member, this CTA's half of its rows) */
 				const uint32_t ntot = (uint32_t)(it.pr >> 8) * S * 32 / (PAIR ? 2 : 1);
 				const uint32_t noff = PAIR ? rank * ntot : 0;
+				const uint32_t shb = mstk ? ntot : C::CHUNK_BYTES;
 				int mfp[EMU_MAXMEM], mrt[EMU_MAXMEM];
-				uint32_t mby[EMU_MAXMEM], mdo[EMU_MAXMEM];
+				uint32_t mby[EMU_MAXMEM], mdo[EMU_MAXMEM], stb = 0;
 #pragma unroll
 				for (int j = 0; j < EMU_MAXMEM; j++) {
 					const emu_member mb = members[it.mfirst + (j < nmem ? j : 0)];
 					mfp[j] = cbs[mb.cblock].first_pair;
 					mrt[j] = mb.n0 / EMU_TM;
 					mby[j] = PAIR ? ntot : (uint32_t)mb.rows * S * 32;
-					mdo[j] = (uint32_t)mb.off * S * 32;
+					mdo[j] = (mstk ? 0u : C::CHUNK_BYTES) + (uint32_t)mb.off * S * 32;
+					stb += j < nmem ? mby[j] : 0;
 				}
+				/* shared side from a's views when it is a's side */
+				const bool sha = (mstk ^ swp) != 0;
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					/* the members' pair lists run in step: pair p of every
-					 * member has member 0's M-side view and K */
+					 * member has member 0's view and K on the shared side */
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
-					const xmgd_view_t wm = swp ? va[pr.aview] : vb[pr.bview];
+					const xmgd_view_t ws = sha ? va[pr.aview] : vb[pr.bview];
 					const int nks = vb[pr.bview].n_ks, nh = nks / 2;
-					const int mtile = it.m0 / EMU_TM + (int)rank;
-					const bool mlive = mtile < wm.n_rt;
-					const uint8_t *gm = reinterpret_cast<const uint8_t *>(wm.slices) +
-					    (size_t)mtile * nks * C::CHUNK_BYTES;
+					const int stile = it.m0 / EMU_TM + (mstk ? 0 : (int)rank);
+					const bool slive = stile < ws.n_rt;
+					const uint8_t *gs = reinterpret_cast<const uint8_t *>(ws.slices) +
+					    (size_t)stile * nks * C::CHUNK_BYTES;
 					const uint8_t *gn[EMU_MAXMEM];
 #pragma unroll
 					for (int j = 0; j < EMU_MAXMEM; j++) {
 						const xmgd_pair_t pj = prs[mfp[j] + p];
-						gn[j] = reinterpret_cast<const uint8_t *>(swp ?
+						gn[j] = reinterpret_cast<const uint8_t *>(sha ?
 						    vb[pj.bview].slices : va[pj.aview].slices) +
 						    (size_t)mrt[j] * nks * C::CHUNK_BYTES + noff;
 					}
@@ -589,15 +602,19 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						uint32_t fb = smem_u32(&bar_full[s]);
 						/* a pair's second M tile may lie past the view: its
 						 * rows are then never stored */
-						mbar_expect_tx(fb, (mlive ? C::CHUNK_BYTES : 0) + ntot);
-						if (mlive)
-							bulk_g2s(dst, gm + (size_t)km * C::CHUNK_BYTES,
-							    C::CHUNK_BYTES, fb);
+						/* the shared side reads at its own K index (the
+						 * M side's or the N side's), the members at the
+						 * other */
+						const int ksh = mstk ? kn : km, kst = mstk ? km : kn;
+						mbar_expect_tx(fb, (slive ? shb : 0) + stb);
+						if (slive)
+							bulk_g2s(dst + (mstk ? C::CHUNK_BYTES : 0u),
+							    gs + (size_t)ksh * C::CHUNK_BYTES, shb, fb);
 #pragma unroll
 						for (int j = 0; j < EMU_MAXMEM; j++)
 							if (j < nmem)
-								bulk_g2s(dst + C::CHUNK_BYTES + mdo[j],
-								    gn[j] + (size_t)kn * C::CHUNK_BYTES, mby[j], fb);
+								bulk_g2s(dst + mdo[j],
+								    gn[j] + (size_t)kst * C::CHUNK_BYTES, mby[j], fb);
 #pragma unroll
 						for (int q = 0; q < NST; q++)
 							if (q == s)
@@ -814,22 +831,43 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				break;
 			const emu_item it = items[t];
 			const int pass = it.pr & 1, swp = (it.pr >> 1) & 1, rows = it.pr >> 8;
+			const int mstk = (it.pr >> 2) & 1;
 			/* this warp's NC columns fall into NC / 16 segments of 16, each
-			 * inside one member (members hold multiples of 16 rows): per
+			 * inside one member's output block (N-stacked members hold
+			 * multiples of 16 columns; M-stacked ones multiples of 32
+			 * lanes, so one member holds all of this warp's lanes): per
 			 * segment the output block, its first pair, its F and the
-			 * N-side row of the segment's first column */
-			int scb[NSEG], sfp[NSEG], sF[NSEG], sq0[NSEG];
-#pragma unroll
-			for (int g = 0; g < NSEG; g++) {
-				const int col = half * NC + g * 16;
+			 * N-side row of the segment's first column; and the M-side
+			 * row of this warp's first lane */
+			int scb[NSEG], sfp[NSEG], sF[NSEG], sq0[NSEG], mrow0;
+			if (mstk) {
+				const int row0 = quad * 32;
 				int j = 0;
 				for (int jj = 1; jj < it.mcount; jj++)
-					j += col >= members[it.mfirst + jj].off;
+					j += row0 >= members[it.mfirst + jj].off;
 				const emu_member mb = members[it.mfirst + j];
-				scb[g] = mb.cblock;
-				sfp[g] = cbs[mb.cblock].first_pair;
-				sF[g] = cbF[mb.cblock];
-				sq0[g] = mb.n0 + col - mb.off;
+#pragma unroll
+				for (int g = 0; g < NSEG; g++) {
+					scb[g] = mb.cblock;
+					sfp[g] = cbs[mb.cblock].first_pair;
+					sF[g] = cbF[mb.cblock];
+					sq0[g] = it.m0 + half * NC + g * 16;
+				}
+				mrow0 = mb.n0 + row0 - mb.off;
+			} else {
+#pragma unroll
+				for (int g = 0; g < NSEG; g++) {
+					const int col = half * NC + g * 16;
+					int j = 0;
+					for (int jj = 1; jj < it.mcount; jj++)
+						j += col >= members[it.mfirst + jj].off;
+					const emu_member mb = members[it.mfirst + j];
+					scb[g] = mb.cblock;
+					sfp[g] = cbs[mb.cblock].first_pair;
+					sF[g] = cbF[mb.cblock];
+					sq0[g] = mb.n0 + col - mb.off;
+				}
+				mrow0 = it.m0 + (int)rank * EMU_TM + quad * 32;
 			}
 			const int npairs = cbs[scb[0]].npairs;
 			long long V[NC];
@@ -951,7 +989,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 			 * this thread's TMEM lane is one M-side row; its columns are
 			 * N-side rows of the segments' output blocks.  Without swap
 			 * the M side is b's free index (j), with swap a's (i). */
-			const int ms = it.m0 + (int)rank * EMU_TM + quad * 32 + lane;
+			const int ms = mrow0 + lane;
 			const bool bz = beta == 0.0;
 			const int cm = cplx ? 2 : 1;
 			/* alpha a normal power of two folds into the exponent and
@@ -1278,14 +1316,19 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 		b.key = ((uint64_t)b.swp << 40) | (uint32_t)(b.swp ? cb.eA : cb.eB);
 		bl.push_back(b);
 	}
-	/* one item per member list (every complex pass) */
-	auto push = [&](int m0, int swp, const std::vector<emu_member> &mem) {
+	/* one item per member list (every complex pass); N-stacked: m0 is the
+	 * M tile and the members' rows add up to N; M-stacked: m0 is the N tile
+	 * and ncols its live rows */
+	auto push = [&](int m0, int swp, const std::vector<emu_member> &mem,
+	    int mstk = 0, int ncols = 0) {
 		int tot = 0;
 		for (const emu_member &x : mem)
 			tot += x.rows;
+		if (mstk)
+			tot = ncols;
 		for (int ps = 0; ps < (cplx ? 2 : 1); ps++) {
 			items.push_back(emu_item{m0, (int)members.size(), (int)mem.size(),
-			    ps | (swp ? 2 : 0) | (tot << 8)});
+			    ps | (swp ? 2 : 0) | (mstk ? 4 : 0) | (tot << 8)});
 			members.insert(members.end(), mem.begin(), mem.end());
 		}
 	};
@@ -1339,6 +1382,9 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 		go[g] = (int)g;
 	std::stable_sort(go.begin(), go.end(),
 	    [&](int x, int y) { return gcost[x] > gcost[y]; });
+	/* merged: partial M tiles wait for the M-stacking pass below */
+	struct tail { int i, m0, n0, ncols; };
+	std::vector<tail> tails;
 	for (int g : go) {
 		int mmax = 0;
 		for (int i : groups[g])
@@ -1348,6 +1394,13 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 				for (int i : groups[g])
 					if (m0 < bl[i].mlen)
 						emit(bl[i], m0);
+				continue;
+			}
+			if (mmax - m0 < EMU_TM) {
+				for (int i : groups[g])
+					for (int n0 = 0; n0 < bl[i].nlen; n0 += EMU_TM)
+						tails.push_back(tail{i, m0, n0, std::min(EMU_TM,
+						    (bl[i].nlen - n0 + 15) / 16 * 16)});
 				continue;
 			}
 			/* full 128-row N tiles alone; the partial ones packed
@@ -1386,6 +1439,65 @@ make_items(const xmgd_contract_t *p, const std::vector<int> &cblocks, int cplx,
 				push(m0, bl[groups[g][0]].swp, mem);
 		}
 	}
+	if (!merged)
+		return;
+	/* M-stacking: the partial M tiles of blocks that share the N side (the
+	 * same N-side view and K at every pair index, the same N tile) fill
+	 * common 128-lane tiles, 32 lanes at a time; a tile left alone runs
+	 * as an ordinary item */
+	std::vector<std::vector<int64_t>> tkey;
+	std::vector<std::vector<int>> tgrp;
+	for (int x = 0; x < (int)tails.size(); x++) {
+		const blk &b = bl[tails[x].i];
+		const xmgd_cblock_t &cb = p->cblocks[b.ci];
+		k.assign({(int64_t)b.swp, tails[x].n0, tails[x].ncols, b.nlen});
+		for (int q = 0; q < cb.npairs; q++) {
+			const xmgd_pair_t &pr = p->pairs[cb.first_pair + q];
+			k.push_back(((int64_t)(b.swp ? pr.bview : pr.aview) << 32) | pr.k);
+		}
+		size_t g = 0;
+		while (g < tkey.size() && tkey[g] != k)
+			g++;
+		if (g == tkey.size()) {
+			tkey.push_back(k);
+			tgrp.push_back({});
+		}
+		tgrp[g].push_back(x);
+	}
+	for (const std::vector<int> &tg : tgrp) {
+		std::vector<emu_member> part;
+		for (int x : tg) {
+			const tail &tl = tails[x];
+			const blk &b = bl[tl.i];
+			part.push_back(emu_member{b.ci, tl.m0, (b.mlen - tl.m0 + 31) / 32 * 32, 0});
+		}
+		std::stable_sort(part.begin(), part.end(),
+		    [](const emu_member &x, const emu_member &y) { return x.rows > y.rows; });
+		std::vector<std::vector<emu_member>> bins;
+		std::vector<int> fill;
+		for (const emu_member &x : part) {
+			size_t b = 0;
+			while (b < bins.size() && (fill[b] + x.rows > EMU_TM ||
+			    (int)bins[b].size() == EMU_MAXMEM))
+				b++;
+			if (b == bins.size()) {
+				bins.push_back({});
+				fill.push_back(0);
+			}
+			emu_member y = x;
+			y.off = fill[b];
+			bins[b].push_back(y);
+			fill[b] += x.rows;
+		}
+		const tail &t0 = tails[tg[0]];
+		const int swp = bl[t0.i].swp;
+		for (const auto &mem : bins) {
+			if (mem.size() == 1)
+				push(mem[0].n0, swp, {emu_member{mem[0].cblock, t0.n0, t0.ncols, 0}});
+			else
+				push(t0.n0, swp, mem, 1, t0.ncols);
+		}
+	}
 }
 
 /* The invariants the kernel's addressing relies on, checked on the host
@@ -1402,6 +1514,36 @@ items_ok(const xmgd_contract_t *p, const std::vector<emu_item> &items,
 			return false;
 		const int swp = (it.pr >> 1) & 1, tot = it.pr >> 8;
 		const xmgd_cblock_t &c0 = p->cblocks[mem[it.mfirst].cblock];
+		if ((it.pr >> 2) & 1) {
+			/* M-stacked: the shared N tile, then 32-lane members */
+			const int nlen = swp ? c0.n : c0.m;
+			if (pair || it.m0 < 0 || it.m0 % EMU_TM || it.m0 >= nlen ||
+			    tot != std::min(EMU_TM, (nlen - it.m0 + 15) / 16 * 16))
+				return false;
+			int off = 0;
+			for (int j = 0; j < it.mcount; j++) {
+				const emu_member &m = mem[it.mfirst + j];
+				if (m.cblock < 0 || m.cblock >= p->ncblocks)
+					return false;
+				const xmgd_cblock_t &cb = p->cblocks[m.cblock];
+				const int ml = swp ? cb.m : cb.n;
+				if ((swp ? cb.n : cb.m) != nlen || cb.npairs != c0.npairs ||
+				    m.off != off || m.rows < 32 || m.rows % 32 || m.n0 < 0 ||
+				    m.n0 % EMU_TM || m.n0 >= ml ||
+				    m.rows != std::min(EMU_TM, (ml - m.n0 + 31) / 32 * 32))
+					return false;
+				for (int q = 0; q < cb.npairs; q++) {
+					const xmgd_pair_t &a = p->pairs[c0.first_pair + q];
+					const xmgd_pair_t &b = p->pairs[cb.first_pair + q];
+					if (a.k != b.k || (swp ? a.bview != b.bview : a.aview != b.aview))
+						return false;
+				}
+				off += m.rows;
+			}
+			if (off > EMU_TM)
+				return false;
+			continue;
+		}
 		const int mlen = swp ? c0.m : c0.n;
 		if (it.m0 < 0 || it.m0 % EMU_TM || it.m0 >= mlen)
 			return false;
