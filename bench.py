@@ -229,8 +229,8 @@ def block_costs(w):
 
 # DRAM bytes (read + write) of one split-precision GEMM launch on the cfg2
 # ladder, from a single-pass ncu capture of that kernel on this workload
-# (the tuned work list; the cost-ordered one reads 128 GB at the same speed)
-GEMM_DRAM_BYTES = 140.78e9 + 0.70118e9
+# (the stacked work list the tuner keeps; the unstacked ones read 128-141 GB)
+GEMM_DRAM_BYTES = 75.93e9 + 0.71307e9
 
 
 def timed_calls(eng, fn, reps=3, warm=5):
@@ -431,6 +431,7 @@ def engine_arm(args, ranks):
         ms = ranks.max(ms)
         return {"ms_per_step": ms / steps, "gemm_ms": float(np.mean(gemm_ms)),
                 "split_ms": float(np.mean(split_ms)), "launches": launches // steps,
+                "gemm_policy": api.last_stats(eng).gemm_policy,
                 "clocks": clocks, "precision_used": api.last_stats(eng).precision_used,
                 "out": W.read_canonical(w.c)}
 
@@ -603,6 +604,9 @@ def engine_arm(args, ranks):
                     "gpu_fp64_vs_cpu_fp64_sample": rel_fp64_vs_cpu if cpu else None},
         "precision_used": "emu64" if emu["precision_used"] == api.PREC_EMU64 else "fp64",
         "phases_ms": {"gemm": emu["gemm_ms"], "split": emu["split_ms"]},
+        "gemm_work_list": {"policy": emu["gemm_policy"],
+                           "note": "autotuned work-list policy of the split-precision GEMM "
+                                   "(6: stacked tiles; 0-2: one output block per tile)"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "out_of_core": ooc,
         "elementwise": elem, "other_configs": configs,
         "gpu_launches": emu["launches"], "clocks": emu["clocks"],

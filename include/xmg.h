@@ -85,7 +85,8 @@ typedef struct {
 	int gemm_launches;       /* kernels launched for the GEMM phase */
 	long long stage_bytes;   /* out-of-core: b bytes streamed into HBM */
 	int stage_batches;       /* out-of-core: batches (0: in-core) */
-	int pad_;
+	int gemm_policy;         /* work-list policy of the split-precision
+	                            GEMM (last batch), -1 if none ran */
 	double ms_stage_wait;    /* out-of-core: host wait for staging beyond
 	                            the overlapped compute, wall clock */
 } xmg_stats_t;

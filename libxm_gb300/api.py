@@ -58,7 +58,7 @@ class Stats(C.Structure):
                 ("n_pairs", C.c_longlong), ("slice_bytes", C.c_longlong),
                 ("precision_used", C.c_int), ("gemm_launches", C.c_int),
                 ("stage_bytes", C.c_longlong), ("stage_batches", C.c_int),
-                ("pad_", C.c_int), ("ms_stage_wait", C.c_double)]
+                ("gemm_policy", C.c_int), ("ms_stage_wait", C.c_double)]
 
 
 _P = C.c_void_p

@@ -35,6 +35,7 @@ int emu_record_gemm(emu_plan *e);
 int emu_finish(emu_plan *e, float gemm_ms, int *nan);
 int64_t emu_slice_bytes(const emu_plan *e);
 int emu_items(const emu_plan *e);
+int emu_policy(const emu_plan *e);
 int emu_current(const emu_plan *e);
 int emu_ncand(const emu_plan *e);
 bool emu_tuned(const emu_plan *e);
@@ -340,6 +341,7 @@ xmgd_plan_run(xmgd_plan *dp, int *precision_used)
 	float ms = 0, ms_split = 0, ms_emu = 0, ms_plain = 0;
 
 	memset(&g_timing, 0, sizeof g_timing);
+	g_timing.gemm_policy = -1;
 	*precision_used = XMG_PREC_FP64;
 	if (dp->ep) {
 		bool moved;
@@ -372,6 +374,7 @@ xmgd_plan_run(xmgd_plan *dp, int *precision_used)
 		g_timing.ms_gemm += ms_emu;
 		g_timing.gemm_launches += 1;
 		g_timing.gemm_items += emu_items(dp->ep);
+		g_timing.gemm_policy = emu_policy(dp->ep);
 		g_timing.slice_bytes = emu_slice_bytes(dp->ep);
 		if ((st = emu_finish(dp->ep, ms_emu, &nan)))
 			return st;

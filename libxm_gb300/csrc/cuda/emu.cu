@@ -1804,6 +1804,7 @@ int emu_record_split(emu_plan *e) { return e->split(e); }
 int emu_record_gemm(emu_plan *e) { return e->gemm(e); }
 int64_t emu_slice_bytes(const emu_plan *e) { return (int64_t)e->slice_bytes; }
 int emu_items(const emu_plan *e) { return e->cand[e->cur].nitems; }
+int emu_policy(const emu_plan *e) { return e->cand[e->cur].policy; }
 
 /* after the stream has drained: flags, then one tuning step with the
  * measured GEMM time of the candidate that ran */

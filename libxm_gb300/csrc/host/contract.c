@@ -1042,6 +1042,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	bstart[nb] = nu;
 	memset(io, 0, sizeof io);
 	memset(&acc, 0, sizeof acc);
+	acc.gemm_policy = -1;
 	xmg_hmap_init(&filt);
 	if ((*st = xmgd_alloc(rbytes, &reg[0])) != XMG_OK ||
 	    (nb > 1 && (*st = xmgd_alloc(rbytes, &reg[1])) != XMG_OK) ||
@@ -1129,6 +1130,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 			acc.ms_gemm += tm.ms_gemm;
 			acc.n_pairs += p.npr;
 			acc.gemm_launches += tm.gemm_launches;
+			acc.gemm_policy = tm.gemm_policy;
 			if (tm.slice_bytes > acc.slice_bytes)
 				acc.slice_bytes = tm.slice_bytes;
 			if (p.npr > 0 && used != XMG_PREC_EMU64)
@@ -1263,6 +1265,7 @@ stats_from(double flops, int ncb, int npr, int precision_used, double t0)
 	g_stats.slice_bytes = tm.slice_bytes;
 	g_stats.precision_used = precision_used;
 	g_stats.gemm_launches = tm.gemm_launches;
+	g_stats.gemm_policy = tm.gemm_policy;
 	(void)t0;
 }
 

@@ -152,6 +152,7 @@ typedef struct {
 	double ms_total, ms_split, ms_gemm;
 	int64_t slice_bytes;
 	int32_t gemm_launches, gemm_items;
+	int32_t gemm_policy;         /* split-precision work list, -1: none */
 } xmgd_timing_t;
 void xmgd_last_timing(xmgd_timing_t *t);
 
