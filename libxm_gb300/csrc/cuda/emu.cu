@@ -600,11 +600,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						const int km = swp ? ks : kb, kn = swp ? kb : ks;
 						uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 						uint32_t fb = smem_u32(&bar_full[s]);
-						/* a pair's second M tile may lie past the view: its
-						 * rows are then never stored */
 						/* the shared side reads at its own K index (the
 						 * M side's or the N side's), the members at the
-						 * other */
+						 * other; a pair's second M tile may lie past the
+						 * view: its rows are then never stored */
 						const int ksh = mstk ? kn : km, kst = mstk ? km : kn;
 						mbar_expect_tx(fb, (slive ? shb : 0) + stb);
 						if (slive)
