@@ -47,32 +47,6 @@ static inline int mt_host(int dbytes, int sbytes)
 }
 constexpr int MAT_MAXQ = 64;       /* slices per CTA at most */
 
-/* asynchronous global -> shared copy of one element (cp.async: no
- * register holds the value while it is in flight) */
-template <int B> __device__ __forceinline__ void cp_async_b(void *s, const void *g);
-template <> __device__ __forceinline__ void cp_async_b<4>(void *s, const void *g)
-{
-	asm volatile("cp.async.ca.shared.global [%0], [%1], 4;"
-	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
-}
-template <> __device__ __forceinline__ void cp_async_b<8>(void *s, const void *g)
-{
-	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
-	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
-}
-template <> __device__ __forceinline__ void cp_async_b<16>(void *s, const void *g)
-{
-	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
-	    :: "r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g) : "memory");
-}
-template <typename T> __device__ __forceinline__ void cp_async_elem(T *s, const T *g)
-{
-	cp_async_b<sizeof(T)>(s, g);
-}
-__device__ __forceinline__ void cp_async_wait_all()
-{
-	asm volatile("cp.async.wait_all;" ::: "memory");
-}
 
 struct task_meta {
 	int64_t first_cta;
