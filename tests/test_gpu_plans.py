@@ -157,3 +157,44 @@ def test_cta_pair_kernel(engine, oracle, gal, oal, monkeypatch):
         engine.check(engine.xmg_set_precision(api.PREC_AUTO))
         w.free()
         wo.free()
+
+
+@pytest.mark.parametrize("policy", [0, 6])
+def test_work_list_policies(engine, oracle, gal, oal, monkeypatch, policy):
+    """A fixed work-list policy (read when a plan is built) runs and gives
+    the oracle's result: 0 (one output block per tile) and 6 (stacked
+    tiles: N-side tails of blocks sharing an M side in common columns,
+    M-side tails of blocks sharing an N side in common lanes); the
+    statistics report the policy that ran."""
+    monkeypatch.setenv("XMG_POLICY", str(policy))
+    w, wo = _pair(engine, oracle, gal, oal, seed=11)
+    try:
+        engine.check(engine.xmg_set_precision(api.PREC_EMU64))
+        wo.run()
+        w.run()
+        st = api.last_stats(engine)
+        assert st.precision_used == api.PREC_EMU64
+        assert st.gemm_policy == policy
+        assert _rel(w, wo) <= REL
+    finally:
+        engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+        w.free()
+        wo.free()
+
+
+def test_stacked_work_list_ring_complex(engine, oracle, monkeypatch):
+    """The stacked work list on the permuted ring term in complex128 (two
+    real passes, beta = 1, transposes on both unfolds and the fold)."""
+    monkeypatch.setenv("XMG_POLICY", "6")
+    eal, oal2 = api.Allocator(engine), api.Allocator(oracle)
+    we = W.cfg3(engine, eal, dtype=api.DOUBLE_COMPLEX, o_blk=6, v_blk=10)
+    wo = W.cfg3(oracle, oal2, dtype=api.DOUBLE_COMPLEX, o_blk=6, v_blk=10)
+    try:
+        wo.run()
+        we.run()
+        st = api.last_stats(engine)
+        assert st.precision_used == api.PREC_EMU64 and st.gemm_policy == 6
+        assert W.rel_frobenius(W.read_canonical(we.c), W.read_canonical(wo.c)) <= REL
+    finally:
+        we.free()
+        wo.free()
