@@ -71,6 +71,14 @@ int xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, const char *idxa, const char *idxb,
     const char *idxc, xmg_pair_cb cb);
 
+/* The split-precision GEMM's work list for one policy (0-2, 6), built and
+ * checked on the host without a device: out = {items, members, items with
+ * more than one member, 1 if every invariant the kernel relies on holds}.
+ * For tests and tuning studies. */
+int xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, int policy, long long out[4]);
+
 /* Statistics of the last xm_contract / xmg_contract on this process. */
 typedef struct {
 	double flops;            /* useful flops (see xmg_contract_flops) */

@@ -1795,6 +1795,38 @@ emu_bind(emu_plan *e, bool *moved)
 	return XMG_OK;
 }
 
+/* the work list of one policy, built and checked on the host (no device) */
+extern "C" int
+xmgd_work_list_check(const xmgd_contract_t *p, int policy, long long out[4])
+{
+	int cplx;
+
+	switch (p->dtype) {
+	case 0: case 2: cplx = 0; break;
+	case 1: case 3: cplx = 1; break;
+	default:
+		return xmg_seterr(XMG_EINVAL, "work list: scalar type");
+	}
+	if (policy < 0 || (policy >= EMU_NPOLICY && !pair_policy(policy) &&
+	    policy != EMU_POL_MERGED))
+		return xmg_seterr(XMG_EINVAL, "work list: no policy %d", policy);
+	std::vector<int> cblocks;
+	for (int i = 0; i < p->ncblocks; i++)
+		if (p->cblocks[i].npairs > 0 && p->emulatable[i])
+			cblocks.push_back(i);
+	std::vector<emu_item> items;
+	std::vector<emu_member> mem;
+	make_items(p, cblocks, cplx, policy, items, mem);
+	long long stacked = 0;
+	for (const emu_item &it : items)
+		stacked += it.mcount > 1;
+	out[0] = (long long)items.size();
+	out[1] = (long long)mem.size();
+	out[2] = stacked;
+	out[3] = items_ok(p, items, mem, pair_policy(policy)) ? 1 : 0;
+	return XMG_OK;
+}
+
 int emu_current(const emu_plan *e) { return e->cur; }
 int emu_ncand(const emu_plan *e) { return (int)e->cand.size(); }
 bool emu_tuned(const emu_plan *e) { return e->tuned != 0; }

@@ -415,6 +415,9 @@ static int
 build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, plan_t *p, int device)
 {
+	/* device: 0 pairs only; 1 the full device plan (blocks staged);
+	 * 2 the full structure with data handles in place of device
+	 * addresses (no device needed: work-list checks) */
 	xm_dim_t *list, nba, nbb, blkc, ia, ib, dims, dA, dB, ka, kb;
 	size_t nlist, nblkk, l, i;
 	struct cand *cand = NULL;
@@ -451,9 +454,9 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			xmg_canon_strides(&dims, sc);
 			cb->crow = mask_table(&p->tabs, &dims, sc, &p->cidxc);
 			cb->ccol = mask_table(&p->tabs, &dims, sc, &p->aidxc);
-			if ((st = xmg_alloc_device_view(c->allocator,
-			    xm_tensor_get_block_data_ptr(c, blkc),
-			    xm_tensor_get_block_bytes(c, blkc), &dptr)) != XMG_OK)
+			dptr = xm_tensor_get_block_data_ptr(c, blkc);
+			if (device == 1 && (st = xmg_alloc_device_view(c->allocator,
+			    dptr, xm_tensor_get_block_bytes(c, blkc), &dptr)) != XMG_OK)
 				break;
 			cb->c_ptr = dptr;
 		}
@@ -544,12 +547,14 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			bcol = mask_table(&p->tabs, &dB, sb, &p->aidxb);
 			pr->arow = arow; pr->acol = acol;
 			pr->brow = brow; pr->bcol = bcol;
-			if ((st = xmg_alloc_device_view(a->allocator, cand[i].da,
-			    xm_tensor_get_block_bytes(a, cand[i].ia), &dptr)))
+			dptr = cand[i].da;
+			if (device == 1 && (st = xmg_alloc_device_view(a->allocator,
+			    cand[i].da, xm_tensor_get_block_bytes(a, cand[i].ia), &dptr)))
 				break;
 			pr->a_ptr = dptr;
-			if ((st = xmg_alloc_device_view(b->allocator, cand[i].db,
-			    xm_tensor_get_block_bytes(b, cand[i].ib), &dptr)))
+			dptr = cand[i].db;
+			if (device == 1 && (st = xmg_alloc_device_view(b->allocator,
+			    cand[i].db, xm_tensor_get_block_bytes(b, cand[i].ib), &dptr)))
 				break;
 			pr->b_ptr = dptr;
 			ea = exp_slot(&p->ea_index, &p->nexp_a, a, cand[i].ia,
@@ -618,6 +623,28 @@ xmg_contract_pairs(const xm_tensor_t *a, const xm_tensor_t *b,
 				cb((size_t)l, pr->al[0], pr->al[1], p.cb[l].m,
 				    p.cb[l].n, pr->k);
 			}
+	}
+	plan_free(&p);
+	return st;
+}
+
+static void fill_contract(xmgd_contract_t *dp, const plan_t *p,
+    xm_scalar_t alpha, xm_scalar_t beta, int prec);
+
+int
+xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, int policy, long long out[4])
+{
+	xmgd_contract_t dp;
+	plan_t p;
+	int st;
+
+	init_plan(&p);
+	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) == XMG_OK &&
+	    (st = build_plan(1, a, b, c, &p, 2)) == XMG_OK) {
+		fill_contract(&dp, &p, 1, 0, XMG_PREC_EMU64);
+		st = xmgd_work_list_check(&dp, policy, out);
 	}
 	plan_free(&p);
 	return st;

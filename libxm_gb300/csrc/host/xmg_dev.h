@@ -137,6 +137,9 @@ typedef struct {
 } xmgd_contract_t;
 
 int xmgd_contract(xmgd_contract_t *plan);
+/* the split-precision work list of one policy, built and checked on the
+ * host: {items, members, stacked items, invariants hold} */
+int xmgd_work_list_check(const xmgd_contract_t *p, int policy, long long out[4]);
 
 /* Reusable device plan of one contraction: the uploaded metadata, operand
  * views and work lists, and the whole launch sequence captured once as a

@@ -214,3 +214,44 @@ def test_autosplit_tiles_opt_in(engine, dims):
         bs.free()
     with pytest.raises(api.XmError):
         engine.check(engine.xmg_block_space_autosplit_tiles(None, 32, 16))
+
+
+def _work_list(engine, w, policy):
+    out = (api.C.c_longlong * 4)()
+    engine.check(engine.xmg_work_list_check(w.a.h, w.b.h, w.c.h, w.idxa.encode(),
+                                            w.idxb.encode(), w.idxc.encode(), policy, out))
+    return list(out)
+
+
+@pytest.mark.parametrize("name", ["cfg2", "cfg3", "cfg5"])
+def test_gemm_work_lists_hold_their_invariants(engine, pagefile, name):
+    """The split-precision GEMM's work lists, built on the host for the
+    full-size structures: every policy's list passes the checks the kernel's
+    addressing relies on (member tiles inside their views and the stage,
+    members sharing the other side pair by pair), and the stacked list
+    (policy 6) holds stacked items, fewer items than policy 2 and never more
+    members than policy 2 has items."""
+    gen = {"cfg2": lambda: W.cfg2(engine, pagefile),
+           "cfg3": lambda: W.cfg3(engine, pagefile, dtype=api.DOUBLE_COMPLEX),
+           "cfg5": lambda: W.cfg5(engine, pagefile, v_blocks=8)}[name]
+    orig_fill = W.fill
+    W.fill = lambda *a, **k: None      # structure only: no data
+    try:
+        w = gen()
+    finally:
+        W.fill = orig_fill
+    try:
+        lists = {pol: _work_list(engine, w, pol) for pol in (0, 1, 2, 6)}
+        for pol, (nitems, nmem, stacked, ok) in lists.items():
+            assert ok == 1, (name, pol)
+            assert nitems > 0
+            if pol != 6:
+                assert nmem == nitems and stacked == 0
+        n2, n6 = lists[2][0], lists[6]
+        if name == "cfg2":
+            assert n6[2] > 0 and n6[0] < n2 and n6[1] <= n2
+        with pytest.raises(api.XmError):
+            _work_list(engine, w, 7)
+    finally:
+        for t in w.tensors():
+            t.free(data=True)
