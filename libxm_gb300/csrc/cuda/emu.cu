@@ -1725,11 +1725,10 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		std::vector<emu_item> items;
 		std::vector<emu_member> mem;
 		make_items(p, cblocks, cplx, pol, items, mem);
-		if (!items_ok(p, items, mem, pair_policy(pol))) {
-			st = xmg_seterr(XMG_EINVAL, "split-precision path: work list %d "
-			    "failed its checks", pol);
-			goto fail;
-		}
+		/* a list that fails its checks is never uploaded; the others
+		 * stand in for it */
+		if (!items_ok(p, items, mem, pair_policy(pol)))
+			continue;
 		bool dup = false;
 		for (size_t l = 0; l < lists.size(); l++)
 			dup |= lists[l].size() == items.size() && mlists[l].size() == mem.size() &&
@@ -1753,6 +1752,11 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		e->cand.push_back(c);
 		lists.push_back(std::move(items));
 		mlists.push_back(std::move(mem));
+	}
+	if (e->cand.empty()) {
+		st = xmg_seterr(XMG_EINVAL, "split-precision path: no work list "
+		    "passed its checks");
+		goto fail;
 	}
 	e->tuned = e->cand.size() <= 1;
 	if ((st = check(cudaMallocHost(&e->h_flags, 2 * sizeof(int)), "flags")) ||
