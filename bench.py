@@ -536,7 +536,8 @@ def engine_arm(args, ranks):
     # bandwidth-bound operations on b (the largest tensor), timed on the
     # device through the public calls: xm_set (write), xm_add without and
     # with a permutation (read a, read b, write a: the gather-transpose
-    # path of unfold/fold)
+    # path of unfold/fold), xm_copy (read, write), xm_mul (read a, read b,
+    # write a), xm_dot (read both, one scalar back)
     elem = None
     if not args.no_elementwise:
         nbytes = sum(w.b.block_size(blk) for blk in w.b.canonical_blocks()) * 8
@@ -546,7 +547,11 @@ def engine_arm(args, ranks):
         for name, fn, traffic in (
                 ("xm_set", lambda: api.set_all(b2, 1.5), nbytes),
                 ("xm_add", lambda: api.add(0.5, b2, 0.25, w.b, "cdab", "cdab"), 3 * nbytes),
-                ("xm_add_permuted", lambda: api.add(0.5, b2, 0.25, w.b, "cdab", "dcab"), 3 * nbytes)):
+                ("xm_add_permuted", lambda: api.add(0.5, b2, 0.25, w.b, "cdab", "dcab"), 3 * nbytes),
+                ("xm_copy", lambda: api.copy(b2, 1.0, w.b, "cdab", "cdab"), 2 * nbytes),
+                ("xm_copy_permuted", lambda: api.copy(b2, 1.0, w.b, "cdab", "dcab"), 2 * nbytes),
+                ("xm_mul", lambda: api.mul(b2, w.b, "cdab", "cdab"), 3 * nbytes),
+                ("xm_dot", lambda: api.dot(b2, w.b, "cdab", "cdab"), 2 * nbytes)):
             fn()
             eng.check(eng.xmg_synchronize())
             eng.check(eng.xmg_timer_start())
