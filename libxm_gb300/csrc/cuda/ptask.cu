@@ -108,7 +108,7 @@ outer_offsets(const xmgd_ptask_t &t, int first_dim, int64_t o, int64_t &od,
 }
 
 template <typename D, typename S, int MODE>
-__global__ void __launch_bounds__(PT_THREADS, MODE == 0 ? 6 : MODE == 3 ? 5 : 1)
+__global__ void __launch_bounds__(PT_THREADS, MODE == 0 ? 6 : MODE == 3 ? 5 : MODE == 2 ? 5 : 1)
 ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
     const task_meta *__restrict__ meta, int ntasks, int64_t cta0,
     double *__restrict__ partial)
@@ -195,6 +195,40 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 						for (int w = 0; w < W; w++)
 							x.v[w] = num<D>::mul(als, y.v[w]);
 						dv[e] = x;
+					}
+					break;
+				case XMGD_OP_MUL:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						vec x = dv[e];
+						const vec y = sv[e];
+#pragma unroll
+						for (int w = 0; w < W; w++)
+							x.v[w] = num<D>::mul(num<D>::mul(al, x.v[w]), y.v[w]);
+						dv[e] = x;
+					}
+					break;
+				case XMGD_OP_DIV:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						vec x = dv[e];
+						const vec y = sv[e];
+#pragma unroll
+						for (int w = 0; w < W; w++)
+							x.v[w] = num<D>::div(x.v[w], num<D>::mul(al, y.v[w]));
+						dv[e] = x;
+					}
+					break;
+				case XMGD_OP_DOT:
+#pragma unroll 4
+					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
+						const vec x = dv[e], y = sv[e];
+#pragma unroll
+						for (int w = 0; w < W; w++) {
+							const D p = num<D>::mul(x.v[w], y.v[w]);
+							dre += num<D>::re(p);
+							dim_ += num<D>::im(p);
+						}
 					}
 					break;
 				default:
