@@ -63,6 +63,7 @@ using namespace xmg;
 
 struct xmgd_plan {
 	int dtype, precision;
+	bool one_shot;                       /* launched directly, once */
 	double alpha[2], beta[2];
 	std::vector<xmgd_cblock_t> cbs;      /* host copies, for the fallback */
 	std::vector<xmgd_pair_t> prs;
@@ -224,6 +225,7 @@ xmgd_plan_create(const xmgd_contract_t *p, xmgd_plan **out)
 	*out = nullptr;
 	dp->dtype = p->dtype;
 	dp->precision = p->precision;
+	dp->one_shot = p->one_shot != 0;
 	memcpy(dp->alpha, p->alpha, sizeof dp->alpha);
 	memcpy(dp->beta, p->beta, sizeof dp->beta);
 	dp->cbs.assign(p->cblocks, p->cblocks + p->ncblocks);
@@ -325,7 +327,7 @@ run_segment(xmgd_plan *dp, int seg, segment &g)
 
 	if (seg_empty(dp, seg))
 		return XMG_OK;
-	if (!graphs_enabled())
+	if (!graphs_enabled() || dp->one_shot)
 		return record(dp, seg);
 	if (!g.x && (st = capture(dp, seg, g)))
 		return st;

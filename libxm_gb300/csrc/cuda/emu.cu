@@ -1712,6 +1712,9 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		known = EMU_POL_MERGED;
 	if (getenv("XMG_POLICY"))	/* one fixed work-list policy */
 		known = atoi(getenv("XMG_POLICY"));
+	/* a plan that runs once has no runs left to tune with: the first
+	 * list that passes its checks */
+	const bool first_only = p->one_shot && known < 0;
 	/* the stacked list first: a plan that runs once (an out-of-core
 	 * batch) never finishes tuning and keeps its first candidate */
 	std::vector<int> pols = {EMU_POL_MERGED, 0, 1, 2};
@@ -1722,6 +1725,8 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	for (int pol : pols) {
 		if (known >= 0 && pol != known)
 			continue;
+		if (first_only && !e->cand.empty())
+			break;
 		std::vector<emu_item> items;
 		std::vector<emu_member> mem;
 		make_items(p, cblocks, cplx, pol, items, mem);

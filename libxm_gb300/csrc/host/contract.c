@@ -1123,6 +1123,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		if ((*st = check_contract(a, b, c, idxa, idxb, idxc, &p)) ==
 		    XMG_OK && (*st = build_plan(alpha, a, b, c, &p, 1)) == XMG_OK) {
 			fill_contract(&dp, &p, alpha, k == 0 ? beta : 1, prec);
+			dp.one_shot = 1;
 			*st = xmgd_plan_create(&dp, &hp);
 		}
 		acc.ms_plan += now_ms() - t0;

@@ -134,6 +134,8 @@ typedef struct {
 	double flops;                /* useful flops (reference counting) */
 	const uint8_t *emulatable;   /* per cblock: every pair factor +-2^t */
 	int precision_used;          /* out: XMG_PREC_FP64 / XMG_PREC_EMU64 */
+	int one_shot;                /* the plan runs once (an out-of-core
+	                                batch): no graphs, no tuning runs */
 } xmgd_contract_t;
 
 int xmgd_contract(xmgd_contract_t *plan);
