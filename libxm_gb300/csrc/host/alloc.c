@@ -31,8 +31,6 @@ struct xm_allocator {
 	unsigned char *used;      /* one bit per page */
 	xmg_hmap_t live;          /* HBM: live handle -> bytes */
 	xmg_hmap_t views;         /* pagefile: handle -> staged device addr */
-	xmg_hmap_t stream;        /* pagefile: handle -> address in the
-	                             current out-of-core batch */
 	xmg_hmap_t bviews;        /* pagefile: handle -> view inside `bulk` */
 	uint64_t bulk;            /* one HBM buffer holding the bulk views */
 };
@@ -58,7 +56,6 @@ xm_allocator_create(const char *path)
 	}
 	xmg_hmap_init(&a->live);
 	xmg_hmap_init(&a->views);
-	xmg_hmap_init(&a->stream);
 	xmg_hmap_init(&a->bviews);
 	a->fd = -1;
 	if (path == NULL) {
@@ -247,8 +244,7 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 		*dptr = h;
 		return XMG_OK;
 	}
-	if (xmg_hmap_get(&a->stream, h, dptr) ||
-	    xmg_hmap_get(&a->views, h, dptr) ||
+	if (xmg_hmap_get(&a->views, h, dptr) ||
 	    xmg_hmap_get(&a->bviews, h, dptr))
 		return XMG_OK;
 	if ((st = xmgd_alloc(bytes, &d)) != XMG_OK)
@@ -338,29 +334,6 @@ xmg_alloc_view_addr(const xm_allocator_t *a, uint64_t h)
 	return 0;
 }
 
-/* Out-of-core batches: while set, blocks of the batch resolve to their
- * addresses in the staging region instead of whole-block views. */
-int
-xmg_alloc_stream_set(xm_allocator_t *a, const uint64_t *h, const uint64_t *d,
-    size_t n)
-{
-	size_t i;
-
-	xmg_hmap_free(&a->stream);
-	xmg_hmap_init(&a->stream);
-	for (i = 0; i < n; i++)
-		if (xmg_hmap_put(&a->stream, h[i], d[i]))
-			return xmg_seterr(XMG_ENOMEM, "out of memory");
-	return XMG_OK;
-}
-
-void
-xmg_alloc_stream_clear(xm_allocator_t *a)
-{
-	xmg_hmap_free(&a->stream);
-	xmg_hmap_init(&a->stream);
-}
-
 void
 xm_allocator_destroy(xm_allocator_t *a)
 {
@@ -382,7 +355,6 @@ xm_allocator_destroy(xm_allocator_t *a)
 	}
 	xmg_hmap_free(&a->live);
 	xmg_hmap_free(&a->views);
-	xmg_hmap_free(&a->stream);
 	xmg_hmap_free(&a->bviews);
 	free(a->path);
 	free(a->used);

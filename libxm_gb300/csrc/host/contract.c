@@ -164,9 +164,8 @@ typedef struct {
 	double flops;
 	uint8_t *emulatable;     /* per cblock */
 	int capem;
-	/* out-of-core: only pairs whose b data is in bfilter; collect lists
-	 * the b data handles (and bytes) of every surviving pair */
-	const xmg_hmap_t *bfilter;
+	/* out-of-core: collect lists the b data handles (and bytes) of
+	 * every surviving pair */
 	int collect;
 	uint64_t *bh, *bsz;
 	size_t nbh, capbh;
@@ -507,8 +506,6 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		for (i = 0; i < nblkk; i++) {
 			if (cand[i].al == 0)
 				continue;
-			if (p->bfilter && !xmg_hmap_get(p->bfilter, cand[i].db, NULL))
-				continue;	/* b block outside this batch */
 			if (p->collect) {
 				if (p->nbh == p->capbh) {
 					p->capbh = p->capbh ? 2 * p->capbh : 256;
@@ -981,6 +978,91 @@ bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
 }
 
 /*
+ * Batch k's contraction, derived from the whole plan (built once per call
+ * with data handles in place of device addresses): the pairs whose b block
+ * is in the batch (dmap: handle -> address in the batch's region), the
+ * operand views those pairs use renumbered in order of first use, a's and
+ * c's blocks at their bulk views.
+ */
+struct batch_buf {
+	xmgd_cblock_t *cb;
+	xmgd_pair_t *pr;
+	xmgd_view_t *va, *vb;
+	int32_t *vamap, *vbmap;
+};
+
+static int
+batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
+    struct batch_buf *bb, xm_scalar_t alpha, xm_scalar_t beta, int prec,
+    xmgd_contract_t *dp)
+{
+	const double mult = xmg_is_complex(pf->type) ? 8.0 : 2.0;
+	double flops = 0;
+	int l, q, v, npr = 0, nva = 0, nvb = 0;
+	uint64_t d;
+
+	for (v = 0; v < pf->nva; v++)
+		bb->vamap[v] = -1;
+	for (v = 0; v < pf->nvb; v++)
+		bb->vbmap[v] = -1;
+	for (l = 0; l < pf->ncb; l++) {
+		const xmgd_cblock_t *cs = &pf->cb[l];
+		xmgd_cblock_t *cd = &bb->cb[l];
+		*cd = *cs;
+		if ((cd->c_ptr = xmg_alloc_view_addr(al, cs->c_ptr)) == 0)
+			return xmg_seterr(XMG_EINVAL, "xm_contract: a block of c "
+			    "without a staged view");
+		cd->first_pair = npr;
+		for (q = 0; q < cs->npairs; q++) {
+			const xmgd_pair_t *ps = &pf->pr[cs->first_pair + q];
+			if (!xmg_hmap_get(dmap, ps->b_ptr, &d))
+				continue;	/* b block outside this batch */
+			xmgd_pair_t *pd = &bb->pr[npr++];
+			*pd = *ps;
+			pd->b_ptr = d;
+			if ((pd->a_ptr = xmg_alloc_view_addr(al, ps->a_ptr)) == 0)
+				return xmg_seterr(XMG_EINVAL, "xm_contract: a block "
+				    "of a without a staged view");
+			if (bb->vamap[ps->aview] < 0) {
+				bb->va[nva] = pf->va[ps->aview];
+				bb->va[nva].ptr = pd->a_ptr;
+				bb->vamap[ps->aview] = nva++;
+			}
+			pd->aview = bb->vamap[ps->aview];
+			if (bb->vbmap[ps->bview] < 0) {
+				bb->vb[nvb] = pf->vb[ps->bview];
+				bb->vb[nvb].ptr = d;
+				bb->vbmap[ps->bview] = nvb++;
+			}
+			pd->bview = bb->vbmap[ps->bview];
+			flops += mult * cs->m * (double)cs->n * ps->k;
+		}
+		cd->npairs = npr - cd->first_pair;
+	}
+	memset(dp, 0, sizeof *dp);
+	dp->dtype = pf->type;
+	dp->precision = prec;
+	xmg_scalar_pack(alpha, dp->alpha);
+	xmg_scalar_pack(beta, dp->beta);
+	dp->ncblocks = pf->ncb;
+	dp->npairs = npr;
+	dp->cblocks = bb->cb;
+	dp->pairs = bb->pr;
+	dp->views_a = bb->va;
+	dp->views_b = bb->vb;
+	dp->nviews_a = nva;
+	dp->nviews_b = nvb;
+	dp->tabs = pf->tabs.v;
+	dp->ntabs = pf->tabs.n;
+	dp->nexp_a = pf->nexp_a;
+	dp->nexp_b = pf->nexp_b;
+	dp->flops = flops;
+	dp->emulatable = pf->emulatable;
+	dp->one_shot = 1;
+	return XMG_OK;
+}
+
+/*
  * Pagefile path.  Returns 0 when the contraction should run through the
  * in-core path (b in GPU memory or b aliasing a or c), else 1 with the
  * status in *st.  b is streamed in batches when its blocks exceed the
@@ -992,6 +1074,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
     const char *idxa, const char *idxb, const char *idxc, int prec, int *st)
 {
 	plan_t p0;
+	struct batch_buf bb = {NULL, NULL, NULL, NULL, NULL, NULL};
 	struct hsz *u = NULL;
 	uint64_t *H = NULL, *SZ = NULL, *OFF = NULL, *D = NULL, total = 0;
 	uint64_t *VH = NULL, *VSZ = NULL, *VD = NULL, *JH = NULL, *JSZ = NULL,
@@ -1013,13 +1096,17 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		g_stage_region = env_bytes("XMG_STAGE_REGION_GB", 32);
 	budget = g_stage_budget;
 	region = g_stage_region;
+	/* the whole plan once, with data handles for addresses; every
+	 * batch's plan is cut from it */
+	double tp = now_ms();
 	init_plan(&p0);
 	p0.collect = 1;
 	if (check_contract(a, b, c, idxa, idxb, idxc, &p0) != XMG_OK ||
-	    build_plan(alpha, a, b, c, &p0, 0) != XMG_OK) {
+	    build_plan(alpha, a, b, c, &p0, 2) != XMG_OK) {
 		plan_free(&p0);
 		return 0;	/* the in-core path reports it */
 	}
+	tp = now_ms() - tp;
 	/* distinct b blocks in file order */
 	if (p0.nbh && (u = malloc(p0.nbh * sizeof *u)) == NULL)
 		xm_fatal("%s: out of memory", __func__);
@@ -1033,7 +1120,6 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 			u[nu++] = u[i];
 	for (i = 0; i < nu; i++)
 		total += u[i].sz;
-	plan_free(&p0);
 	/* within the budget b is staged whole: one batch, still read by the
 	 * parallel readers */
 	if (total <= budget)
@@ -1070,6 +1156,15 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	memset(io, 0, sizeof io);
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;
+	acc.ms_plan = tp;
+	bb.cb = malloc((p0.ncb + 1) * sizeof *bb.cb);
+	bb.pr = malloc((p0.npr + 1) * sizeof *bb.pr);
+	bb.va = malloc((p0.nva + 1) * sizeof *bb.va);
+	bb.vb = malloc((p0.nvb + 1) * sizeof *bb.vb);
+	bb.vamap = malloc((p0.nva + 1) * sizeof *bb.vamap);
+	bb.vbmap = malloc((p0.nvb + 1) * sizeof *bb.vbmap);
+	if (!bb.cb || !bb.pr || !bb.va || !bb.vb || !bb.vamap || !bb.vbmap)
+		xm_fatal("%s: out of memory", __func__);
 	xmg_hmap_init(&filt);
 	if ((*st = xmgd_alloc(rbytes, &reg[0])) != XMG_OK ||
 	    (nb > 1 && (*st = xmgd_alloc(rbytes, &reg[1])) != XMG_OK) ||
@@ -1106,7 +1201,6 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		struct io_job *nx = &io[(k + 1) & 1];
 		xmgd_contract_t dp;
 		xmgd_plan_t *hp = NULL;
-		plan_t p;
 		int used = XMG_PREC_FP64;
 		double t0 = now_ms();
 
@@ -1114,18 +1208,10 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		xmg_hmap_free(&filt);
 		xmg_hmap_init(&filt);
 		for (i = bstart[k]; i < bstart[k + 1]; i++)
-			xmg_hmap_put(&filt, H[i], 1);
-		if ((*st = xmg_alloc_stream_set(b->allocator, H + bstart[k],
-		    D + bstart[k], bstart[k + 1] - bstart[k])) != XMG_OK)
-			break;
-		init_plan(&p);
-		p.bfilter = &filt;
-		if ((*st = check_contract(a, b, c, idxa, idxb, idxc, &p)) ==
-		    XMG_OK && (*st = build_plan(alpha, a, b, c, &p, 1)) == XMG_OK) {
-			fill_contract(&dp, &p, alpha, k == 0 ? beta : 1, prec);
-			dp.one_shot = 1;
+			xmg_hmap_put(&filt, H[i], D[i]);
+		if ((*st = batch_plan(&p0, &filt, a->allocator, &bb, alpha,
+		    k == 0 ? beta : 1, prec, &dp)) == XMG_OK)
 			*st = xmgd_plan_create(&dp, &hp);
-		}
 		acc.ms_plan += now_ms() - t0;
 		/* batch k's data in place (only batch 0 can still be loading:
 		 * later batches were joined at the end of the previous round),
@@ -1152,20 +1238,18 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		if (*st == XMG_OK) {
 			xmgd_timing_t tm;
 			xmgd_last_timing(&tm);
-			acc.flops += p.flops;
+			acc.flops += dp.flops;
 			acc.ms_device += tm.ms_total;
 			acc.ms_split += tm.ms_split;
 			acc.ms_gemm += tm.ms_gemm;
-			acc.n_pairs += p.npr;
+			acc.n_pairs += dp.npairs;
 			acc.gemm_launches += tm.gemm_launches;
 			acc.gemm_policy = tm.gemm_policy;
 			if (tm.slice_bytes > acc.slice_bytes)
 				acc.slice_bytes = tm.slice_bytes;
-			if (p.npr > 0 && used != XMG_PREC_EMU64)
+			if (dp.npairs > 0 && used != XMG_PREC_EMU64)
 				used_all = XMG_PREC_FP64;
 		}
-		plan_free(&p);
-		xmg_alloc_stream_clear(b->allocator);
 		t0 = now_ms();
 		if (k + 1 < nb) {
 			int s2 = io_join(nx);
@@ -1189,7 +1273,6 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	acc.ms_stage_wait = tw;
 	g_stats = acc;
 out_free:
-	xmg_alloc_stream_clear(b->allocator);
 	xmg_hmap_free(&filt);
 	if (reg[0])
 		xmgd_free(reg[0]);
@@ -1198,6 +1281,9 @@ out_free:
 	*st = commit_c(c, *st);
 	xmg_alloc_release_views(a->allocator, 0);
 out:
+	plan_free(&p0);
+	free(bb.cb); free(bb.pr); free(bb.va); free(bb.vb);
+	free(bb.vamap); free(bb.vbmap);
 	free(u); free(H); free(SZ); free(OFF); free(D); free(bstart);
 	free(VH); free(VSZ); free(VD); free(JH); free(JSZ); free(JD);
 	return 1;

@@ -77,9 +77,6 @@ int xmg_alloc_bulk_views(xm_allocator_t *a, uint64_t bulk, const uint64_t *h,
     const uint64_t *d, size_t n);
 uint64_t xmg_alloc_view_addr(const xm_allocator_t *a, uint64_t h);
 int xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes);
-int xmg_alloc_stream_set(xm_allocator_t *a, const uint64_t *h,
-    const uint64_t *d, size_t n);
-void xmg_alloc_stream_clear(xm_allocator_t *a);
 
 /* Permuted-copy task helpers (blockops.c). */
 /* Normalise an iteration space: drop extent-1 dimensions and merge
