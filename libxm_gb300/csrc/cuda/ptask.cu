@@ -92,6 +92,69 @@ struct elem_op {
 	}
 };
 
+/*
+ * Flat runs with 16-byte accesses.  Each thread issues the loads of U
+ * vectors (of both runs) before any of its stores: stores to dst may alias
+ * src as far as the compiler knows, so a plain loop keeps one iteration's
+ * loads in flight at a time.
+ */
+template <typename D> struct alignas(16) vec16 { D v[16 / sizeof(D)]; };
+
+template <int OP, typename D>
+__device__ inline void
+flat_vec(vec16<D> *dv, const vec16<D> *sv, int nv, const D al, const D be,
+    double &dre, double &dim_)
+{
+	constexpr int W = 16 / sizeof(D), U = 4;
+	constexpr bool RD = OP != XMGD_OP_COPY && OP != XMGD_OP_SET;
+	constexpr bool RS = OP != XMGD_OP_SET && OP != XMGD_OP_SCALE;
+	constexpr bool WR = OP != XMGD_OP_DOT;
+
+	for (int e0 = threadIdx.x; e0 < nv; e0 += U * PT_THREADS) {
+		vec16<D> x[U], y[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			const int e = e0 + u * PT_THREADS;
+			if (e < nv) {
+				if (RD)
+					x[u] = dv[e];
+				if (RS)
+					y[u] = sv[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			const int e = e0 + u * PT_THREADS;
+			if (e >= nv)
+				break;
+#pragma unroll
+			for (int w = 0; w < W; w++) {
+				D &xv = x[u].v[w];
+				if (OP == XMGD_OP_SET)
+					xv = al;
+				else if (OP == XMGD_OP_SCALE)
+					xv = num<D>::mul(al, xv);
+				else if (OP == XMGD_OP_AXPY)
+					xv = num<D>::add(num<D>::mul(al, xv),
+					    num<D>::mul(be, y[u].v[w]));
+				else if (OP == XMGD_OP_COPY)
+					xv = num<D>::mul(al, y[u].v[w]);
+				else if (OP == XMGD_OP_MUL)
+					xv = num<D>::mul(num<D>::mul(al, xv), y[u].v[w]);
+				else if (OP == XMGD_OP_DIV)
+					xv = num<D>::div(xv, num<D>::mul(al, y[u].v[w]));
+				else {
+					const D pr = num<D>::mul(xv, y[u].v[w]);
+					dre += num<D>::re(pr);
+					dim_ += num<D>::im(pr);
+				}
+			}
+			if (WR)
+				dv[e] = x[u];
+		}
+	}
+}
+
 static __device__ inline void
 outer_offsets(const xmgd_ptask_t &t, int first_dim, int64_t o, int64_t &od,
     int64_t &os)
@@ -133,8 +196,8 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 	double dre = 0, dim_ = 0;
 
 	if constexpr (MODE == 2) {
-		/* flat: consecutive threads take consecutive elements, four
-		 * loads in flight each, the op resolved outside the loop */
+		/* flat: consecutive threads take consecutive elements, the op
+		 * resolved outside the loop */
 		const int64_t base = local * FLAT_ELEMS;
 		const int n = (int)(t.size[0] - base < FLAT_ELEMS ? t.size[0] - base :
 		    FLAT_ELEMS);
@@ -145,91 +208,34 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 			/* 16-byte accesses when both runs start on a 16-byte
 			 * boundary (whole blocks do), scalar tail */
 			constexpr int W = 16 / sizeof(D);
-			struct alignas(16) vec { D v[W]; };
 			const bool al16 = ((reinterpret_cast<uintptr_t>(dp) |
 			    reinterpret_cast<uintptr_t>(sp)) & 15) == 0;
 			const int nv = n / W;
-			vec *dv = reinterpret_cast<vec *>(dp);
-			const vec *sv = reinterpret_cast<const vec *>(sp);
+			vec16<D> *dv = reinterpret_cast<vec16<D> *>(dp);
+			const vec16<D> *sv = reinterpret_cast<const vec16<D> *>(sp);
 			done = al16;
 			if (al16) {
 				switch (op) {
-				case XMGD_OP_SET: {
-					vec a;
-#pragma unroll
-					for (int w = 0; w < W; w++)
-						a.v[w] = al;
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS)
-						dv[e] = a;
+				case XMGD_OP_SET:
+					flat_vec<XMGD_OP_SET>(dv, sv, nv, al, be, dre, dim_);
 					break;
-				}
 				case XMGD_OP_SCALE:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						vec x = dv[e];
-#pragma unroll
-						for (int w = 0; w < W; w++)
-							x.v[w] = num<D>::mul(al, x.v[w]);
-						dv[e] = x;
-					}
+					flat_vec<XMGD_OP_SCALE>(dv, sv, nv, al, be, dre, dim_);
 					break;
 				case XMGD_OP_AXPY:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						vec x = dv[e];
-						const vec y = sv[e];
-#pragma unroll
-						for (int w = 0; w < W; w++)
-							x.v[w] = num<D>::add(num<D>::mul(al, x.v[w]),
-							    num<D>::mul(be, y.v[w]));
-						dv[e] = x;
-					}
+					flat_vec<XMGD_OP_AXPY>(dv, sv, nv, al, be, dre, dim_);
 					break;
 				case XMGD_OP_COPY:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						const vec y = sv[e];
-						vec x;
-#pragma unroll
-						for (int w = 0; w < W; w++)
-							x.v[w] = num<D>::mul(als, y.v[w]);
-						dv[e] = x;
-					}
+					flat_vec<XMGD_OP_COPY>(dv, sv, nv, als, be, dre, dim_);
 					break;
 				case XMGD_OP_MUL:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						vec x = dv[e];
-						const vec y = sv[e];
-#pragma unroll
-						for (int w = 0; w < W; w++)
-							x.v[w] = num<D>::mul(num<D>::mul(al, x.v[w]), y.v[w]);
-						dv[e] = x;
-					}
+					flat_vec<XMGD_OP_MUL>(dv, sv, nv, al, be, dre, dim_);
 					break;
 				case XMGD_OP_DIV:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						vec x = dv[e];
-						const vec y = sv[e];
-#pragma unroll
-						for (int w = 0; w < W; w++)
-							x.v[w] = num<D>::div(x.v[w], num<D>::mul(al, y.v[w]));
-						dv[e] = x;
-					}
+					flat_vec<XMGD_OP_DIV>(dv, sv, nv, al, be, dre, dim_);
 					break;
 				case XMGD_OP_DOT:
-#pragma unroll 4
-					for (int e = threadIdx.x; e < nv; e += PT_THREADS) {
-						const vec x = dv[e], y = sv[e];
-#pragma unroll
-						for (int w = 0; w < W; w++) {
-							const D p = num<D>::mul(x.v[w], y.v[w]);
-							dre += num<D>::re(p);
-							dim_ += num<D>::im(p);
-						}
-					}
+					flat_vec<XMGD_OP_DOT>(dv, sv, nv, al, be, dre, dim_);
 					break;
 				default:
 					done = false;
