@@ -422,7 +422,7 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	struct cand *cand = NULL;
 	xmg_hmap_t merge;
 	int64_t sa[XM_MAX_DIM], sb[XM_MAX_DIM], sc[XM_MAX_DIM];
-	int32_t crow, ccol, arow, acol, brow, bcol, ea = 0, eb = 0;
+	int32_t arow, acol, brow, bcol, ea = 0, eb = 0;
 	struct xmg_block *ba, *bb;
 	uint64_t rep, dptr;
 	xmgd_cblock_t *cb;
@@ -659,10 +659,12 @@ xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
  * ordinary contraction restricted to the merged pairs whose b data lies in
  * the batch (pairs merge only over equal b data, so the restriction
  * commutes with merging); beta is applied by the first batch and the later
- * ones accumulate with beta = 1.  a's and c's canonical blocks are staged
- * whole, as views in one HBM buffer, by the same readers together with
- * batch 0 while batch 0's plan is built; c is written back by them in
- * reverse (side-stream fetches into the pinned chunks, pwrite).
+ * ones accumulate with beta = 1.  The plan is built once per call, with data
+ * handles for addresses, and each batch's plan cut from it.  a's and c's
+ * canonical blocks are staged whole, as views in one HBM buffer, by the same
+ * readers together with batch 0 while batch 0's plan is cut; c is written
+ * back by them in reverse (side-stream fetches into the pinned chunks,
+ * pwrite).
  */
 #define STAGE_CHUNK ((size_t)64 << 20)
 #define STAGE_ALIGN 256
@@ -991,6 +993,57 @@ struct batch_buf {
 	int32_t *vamap, *vbmap;
 };
 
+static void
+batch_buf_alloc(struct batch_buf *bb, const plan_t *p)
+{
+	bb->cb = malloc((p->ncb + 1) * sizeof *bb->cb);
+	bb->pr = malloc((p->npr + 1) * sizeof *bb->pr);
+	bb->va = malloc((p->nva + 1) * sizeof *bb->va);
+	bb->vb = malloc((p->nvb + 1) * sizeof *bb->vb);
+	bb->vamap = malloc((p->nva + 1) * sizeof *bb->vamap);
+	bb->vbmap = malloc((p->nvb + 1) * sizeof *bb->vbmap);
+	if (!bb->cb || !bb->pr || !bb->va || !bb->vb || !bb->vamap || !bb->vbmap)
+		xm_fatal("%s: out of memory", __func__);
+}
+
+static void
+batch_buf_free(struct batch_buf *bb)
+{
+	free(bb->cb); free(bb->pr); free(bb->va); free(bb->vb);
+	free(bb->vamap); free(bb->vbmap);
+	memset(bb, 0, sizeof *bb);
+}
+
+/* a data handle's device address: its staged view, or the handle itself
+ * when there is no allocator (host-side checks) */
+static uint64_t
+handle_addr(const xm_allocator_t *al, uint64_t h)
+{
+	return al ? xmg_alloc_view_addr(al, h) : h;
+}
+
+/* the distinct b blocks of a collected plan, in handle (file) order */
+static size_t
+distinct_b(const plan_t *p, struct hsz **out)
+{
+	struct hsz *u = NULL;
+	size_t i, nu = 0;
+
+	if (p->nbh && (u = malloc(p->nbh * sizeof *u)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < p->nbh; i++) {
+		u[i].h = p->bh[i];
+		u[i].sz = p->bsz[i];
+	}
+	if (p->nbh)
+		qsort(u, p->nbh, sizeof *u, cmp_hsz);
+	for (i = 0; i < p->nbh; i++)
+		if (nu == 0 || u[nu - 1].h != u[i].h)
+			u[nu++] = u[i];
+	*out = u;
+	return nu;
+}
+
 static int
 batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
     struct batch_buf *bb, xm_scalar_t alpha, xm_scalar_t beta, int prec,
@@ -1009,7 +1062,7 @@ batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
 		const xmgd_cblock_t *cs = &pf->cb[l];
 		xmgd_cblock_t *cd = &bb->cb[l];
 		*cd = *cs;
-		if ((cd->c_ptr = xmg_alloc_view_addr(al, cs->c_ptr)) == 0)
+		if ((cd->c_ptr = handle_addr(al, cs->c_ptr)) == 0)
 			return xmg_seterr(XMG_EINVAL, "xm_contract: a block of c "
 			    "without a staged view");
 		cd->first_pair = npr;
@@ -1020,7 +1073,7 @@ batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
 			xmgd_pair_t *pd = &bb->pr[npr++];
 			*pd = *ps;
 			pd->b_ptr = d;
-			if ((pd->a_ptr = xmg_alloc_view_addr(al, ps->a_ptr)) == 0)
+			if ((pd->a_ptr = handle_addr(al, ps->a_ptr)) == 0)
 				return xmg_seterr(XMG_EINVAL, "xm_contract: a block "
 				    "of a without a staged view");
 			if (bb->vamap[ps->aview] < 0) {
@@ -1060,6 +1113,128 @@ batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
 	dp->emulatable = pf->emulatable;
 	dp->one_shot = 1;
 	return XMG_OK;
+}
+
+/* a view of a batch plan against the whole plan's: equal but for the
+ * address, which is the pair's (field by field: the structs have padding) */
+static int
+same_view(const xmgd_view_t *x, const xmgd_view_t *y, uint64_t ptr)
+{
+	return x->ptr == ptr && x->k == y->k && x->mn == y->mn &&
+	    x->rowtab == y->rowtab && x->coltab == y->coltab &&
+	    x->exptab == y->exptab && x->n_rt == y->n_rt &&
+	    x->n_ks == y->n_ks && x->kfast == y->kfast && x->cplx == y->cplx &&
+	    x->khp == y->khp && x->kcontig == y->kcontig &&
+	    x->slices == y->slices;
+}
+
+/* a pair of a batch plan against the whole plan's, view ids aside */
+static int
+same_pair(const xmgd_pair_t *x, const xmgd_pair_t *y)
+{
+	return x->a_ptr == y->a_ptr && x->b_ptr == y->b_ptr && x->k == y->k &&
+	    x->arow == y->arow && x->acol == y->acol && x->brow == y->brow &&
+	    x->bcol == y->bcol && x->esign == y->esign &&
+	    x->eshift == y->eshift && x->al[0] == y->al[0] &&
+	    x->al[1] == y->al[1];
+}
+
+int
+xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, int nbatch, int policy, long long out[4])
+{
+	plan_t p;
+	struct batch_buf bb;
+	struct hsz *u = NULL;
+	xmg_hmap_t dmap;
+	xmgd_contract_t dp;
+	unsigned char *used = NULL;
+	double flops = 0;
+	long long wl[4], npairs = 0, items = 0;
+	size_t nu, i, k;
+	int st, l, j, q, ok = 1;
+
+	memset(out, 0, 4 * sizeof *out);
+	if (nbatch < 1)
+		return xmg_seterr(XMG_EINVAL, "xmg_batch_plan_check: nbatch < 1");
+	init_plan(&p);
+	p.collect = 1;
+	if ((st = check_contract(a, b, c, idxa, idxb, idxc, &p)) != XMG_OK ||
+	    (st = build_plan(1, a, b, c, &p, 2)) != XMG_OK) {
+		plan_free(&p);
+		return st;
+	}
+	nu = distinct_b(&p, &u);
+	batch_buf_alloc(&bb, &p);
+	if ((used = calloc(p.npr + 1, 1)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	xmg_hmap_init(&dmap);
+	for (k = 0; k < (size_t)nbatch && st == XMG_OK; k++) {
+		/* batch k: the k-th of nbatch equal runs of b's blocks */
+		xmg_hmap_free(&dmap);
+		xmg_hmap_init(&dmap);
+		for (i = nu * k / nbatch; i < nu * (k + 1) / nbatch; i++)
+			if (xmg_hmap_put(&dmap, u[i].h, u[i].h))
+				xm_fatal("%s: out of memory", __func__);
+		if ((st = batch_plan(&p, &dmap, NULL, &bb, 1, k == 0 ? 0 : 1,
+		    XMG_PREC_EMU64, &dp)) != XMG_OK)
+			break;
+		/* each pair of the batch is a later pair of its output block
+		 * in the whole plan, with b in the batch, used by no other
+		 * batch, with the same views */
+		for (l = 0; l < dp.ncblocks; l++) {
+			const xmgd_cblock_t *cs = &p.cb[l], *cd = &dp.cblocks[l];
+			if (cd->m != cs->m || cd->n != cs->n ||
+			    cd->c_ptr != cs->c_ptr || cd->eA != cs->eA ||
+			    cd->eB != cs->eB)
+				ok = 0;
+			for (j = 0, q = 0; j < cd->npairs; j++, q++) {
+				const xmgd_pair_t *pd = &dp.pairs[cd->first_pair + j];
+				const xmgd_pair_t *ps;
+				for (; q < cs->npairs; q++)
+					if (same_pair(pd, &p.pr[cs->first_pair + q]))
+						break;
+				if (q == cs->npairs) {
+					ok = 0;
+					break;
+				}
+				ps = &p.pr[cs->first_pair + q];
+				if (used[cs->first_pair + q]++ ||
+				    !xmg_hmap_get(&dmap, ps->b_ptr, NULL) ||
+				    pd->aview < 0 || pd->aview >= dp.nviews_a ||
+				    pd->bview < 0 || pd->bview >= dp.nviews_b ||
+				    !same_view(&dp.views_a[pd->aview], &p.va[ps->aview],
+				    pd->a_ptr) ||
+				    !same_view(&dp.views_b[pd->bview], &p.vb[ps->bview],
+				    pd->b_ptr))
+					ok = 0;
+			}
+		}
+		npairs += dp.npairs;
+		flops += dp.flops;
+		if ((st = xmgd_work_list_check(&dp, policy, wl)) != XMG_OK)
+			break;
+		items += wl[0];
+		ok = ok && wl[3];
+	}
+	if (st == XMG_OK) {
+		for (i = 0; i < (size_t)p.npr; i++)
+			if (used[i] != 1)
+				ok = 0;
+		if (npairs != p.npr || flops != p.flops)
+			ok = 0;
+		out[0] = nbatch;
+		out[1] = npairs;
+		out[2] = items;
+		out[3] = ok;
+	}
+	xmg_hmap_free(&dmap);
+	free(used);
+	free(u);
+	batch_buf_free(&bb);
+	plan_free(&p);
+	return st;
 }
 
 /*
@@ -1108,16 +1283,14 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	}
 	tp = now_ms() - tp;
 	/* distinct b blocks in file order */
-	if (p0.nbh && (u = malloc(p0.nbh * sizeof *u)) == NULL)
-		xm_fatal("%s: out of memory", __func__);
-	for (i = 0; i < p0.nbh; i++) {
-		u[i].h = p0.bh[i];
-		u[i].sz = p0.bsz[i];
+	nu = distinct_b(&p0, &u);
+	if (nu == 0) {
+		/* no GEMMs (alpha = 0 or no nonzero pair): the in-core path
+		 * applies beta to c */
+		free(u);
+		plan_free(&p0);
+		return 0;
 	}
-	qsort(u, p0.nbh, sizeof *u, cmp_hsz);
-	for (i = 0; i < p0.nbh; i++)
-		if (nu == 0 || u[nu - 1].h != u[i].h)
-			u[nu++] = u[i];
 	for (i = 0; i < nu; i++)
 		total += u[i].sz;
 	/* within the budget b is staged whole: one batch, still read by the
@@ -1157,14 +1330,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;
 	acc.ms_plan = tp;
-	bb.cb = malloc((p0.ncb + 1) * sizeof *bb.cb);
-	bb.pr = malloc((p0.npr + 1) * sizeof *bb.pr);
-	bb.va = malloc((p0.nva + 1) * sizeof *bb.va);
-	bb.vb = malloc((p0.nvb + 1) * sizeof *bb.vb);
-	bb.vamap = malloc((p0.nva + 1) * sizeof *bb.vamap);
-	bb.vbmap = malloc((p0.nvb + 1) * sizeof *bb.vbmap);
-	if (!bb.cb || !bb.pr || !bb.va || !bb.vb || !bb.vamap || !bb.vbmap)
-		xm_fatal("%s: out of memory", __func__);
+	batch_buf_alloc(&bb, &p0);
 	xmg_hmap_init(&filt);
 	if ((*st = xmgd_alloc(rbytes, &reg[0])) != XMG_OK ||
 	    (nb > 1 && (*st = xmgd_alloc(rbytes, &reg[1])) != XMG_OK) ||
@@ -1208,7 +1374,8 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 		xmg_hmap_free(&filt);
 		xmg_hmap_init(&filt);
 		for (i = bstart[k]; i < bstart[k + 1]; i++)
-			xmg_hmap_put(&filt, H[i], D[i]);
+			if (xmg_hmap_put(&filt, H[i], D[i]))
+				xm_fatal("%s: out of memory", __func__);
 		if ((*st = batch_plan(&p0, &filt, a->allocator, &bb, alpha,
 		    k == 0 ? beta : 1, prec, &dp)) == XMG_OK)
 			*st = xmgd_plan_create(&dp, &hp);
@@ -1282,8 +1449,7 @@ out_free:
 	xmg_alloc_release_views(a->allocator, 0);
 out:
 	plan_free(&p0);
-	free(bb.cb); free(bb.pr); free(bb.va); free(bb.vb);
-	free(bb.vamap); free(bb.vbmap);
+	batch_buf_free(&bb);
 	free(u); free(H); free(SZ); free(OFF); free(D); free(bstart);
 	free(VH); free(VSZ); free(VD); free(JH); free(JSZ); free(JD);
 	return 1;

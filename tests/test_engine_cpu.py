@@ -255,3 +255,42 @@ def test_gemm_work_lists_hold_their_invariants(engine, pagefile, name):
     finally:
         for t in w.tensors():
             t.free(data=True)
+
+
+@pytest.mark.parametrize("name,nbatch", [("cfg2", 1), ("cfg2", 4), ("cfg2", 13),
+                                         ("cfg3", 5), ("cfg5", 3)])
+def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbatch):
+    """The out-of-core path builds the whole plan once and cuts each batch's
+    plan from it.  Cut on the host for b's blocks in nbatch runs: every
+    merged pair lands in exactly one batch, in its output block's order,
+    with its views and tables; the flops add up to the whole plan's; every
+    batch's stacked work list holds the kernel's invariants."""
+    gen = {"cfg2": lambda: W.cfg2(engine, pagefile),
+           "cfg3": lambda: W.cfg3(engine, pagefile, dtype=api.DOUBLE_COMPLEX),
+           "cfg5": lambda: W.cfg5(engine, pagefile, v_blocks=8)}[name]
+    orig_fill = W.fill
+    W.fill = lambda *a, **k: None      # structure only: no data
+    try:
+        w = gen()
+    finally:
+        W.fill = orig_fill
+    try:
+        args = (w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+        out = (api.C.c_longlong * 4)()
+        engine.check(engine.xmg_batch_plan_check(*args, nbatch, 6, out))
+        batches, npairs, items, ok = list(out)
+        assert ok == 1 and batches == nbatch
+        whole = _work_list(engine, w, 6)
+        assert whole[3] == 1
+        pairs = H.pair_structure_engine(engine, w.a, w.b, w.c, w.idxa, w.idxb, w.idxc)
+        assert npairs == len(pairs)
+        # one batch is the whole plan: the same work list
+        if nbatch == 1:
+            assert items == whole[0]
+        else:
+            assert items >= whole[0]
+        with pytest.raises(api.XmError):
+            engine.check(engine.xmg_batch_plan_check(*args, 0, 6, out))
+    finally:
+        for t in w.tensors():
+            t.free(data=True)

@@ -246,12 +246,16 @@ def test_cfg2_scaled_golden(engine, gal):
 
 
 def test_pagefile_allocator_contract(engine, oracle, oal):
-    """Tensors in a host pagefile: the engine stages blocks into HBM."""
+    """Tensors in a host pagefile: the engine stages blocks into HBM (with
+    alpha = 0 no GEMM runs and only beta is applied to c)."""
     d = tempfile.mkdtemp()
     pal = api.Allocator(engine, os.path.join(d, "xmpagefile"))
     for ci in (35, 38, 45):
-        x = H.run_contract_case(engine, pal, cases.CONTRACT_TESTS[ci], api.DOUBLE, 1 + ci, 0.5, 0.25)
-        y = H.run_contract_case(oracle, oal, cases.CONTRACT_TESTS[ci], api.DOUBLE, 1 + ci, 0.5, 0.25)
-        _check(x, y, api.DOUBLE)
+        for alpha, beta in ((0.5, 0.25), (0.0, 0.25), (0.0, 0.0)):
+            x = H.run_contract_case(engine, pal, cases.CONTRACT_TESTS[ci], api.DOUBLE, 1 + ci,
+                                    alpha, beta)
+            y = H.run_contract_case(oracle, oal, cases.CONTRACT_TESTS[ci], api.DOUBLE, 1 + ci,
+                                    alpha, beta)
+            _check(x, y, api.DOUBLE)
     pal.destroy()
     os.rmdir(d)
