@@ -294,3 +294,27 @@ def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbat
     finally:
         for t in w.tensors():
             t.free(data=True)
+
+
+@pytest.mark.parametrize("ci", range(len(cases.CONTRACT_TESTS)))
+def test_plan_checks_on_reference_cases(engine, pagefile, ci):
+    """Every contraction case of the reference's test driver, all four
+    scalar types: each work-list policy of the split-precision GEMM holds
+    the kernel's invariants, and the out-of-core batch plans for b's blocks
+    in 1, 2 and 5 runs partition the whole plan."""
+    make, ia, ib, ic = cases.CONTRACT_TESTS[ci]
+    out = (api.C.c_longlong * 4)()
+    for dt in H.TYPES:
+        a, b, c = make(engine, pagefile, dt)
+        try:
+            args = (a.h, b.h, c.h, ia.encode(), ib.encode(), ic.encode())
+            for pol in (0, 1, 2, 6):
+                engine.check(engine.xmg_work_list_check(*args, pol, out))
+                assert out[3] == 1, (dt, pol)
+            npairs = len(H.pair_structure_engine(engine, a, b, c, ia, ib, ic))
+            for nbatch in (1, 2, 5):
+                engine.check(engine.xmg_batch_plan_check(*args, nbatch, 6, out))
+                assert out[3] == 1 and out[1] == npairs, (dt, nbatch)
+        finally:
+            for t in (a, b, c):
+                t.free()
