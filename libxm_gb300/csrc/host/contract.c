@@ -81,7 +81,7 @@ static int32_t
 tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 {
 	uint64_t h = 0x9e3779b97f4a7c15ULL, slot;
-	int64_t total = 1, e, r, o;
+	int64_t total = 1, e, r;
 	struct tabdesc *t;
 	int d;
 
@@ -120,13 +120,23 @@ tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 	memcpy(t->size, size, (size_t)nd * sizeof *size);
 	memcpy(t->stride, stride, (size_t)nd * sizeof *stride);
 	t->off = (int32_t)p->n;
-	for (e = 0; e < total; e++) {
-		r = e; o = 0;
-		for (d = 0; d < nd; d++) {
-			o += (r % size[d]) * stride[d];
-			r /= size[d];
+	if (nd == 0)
+		p->v[p->n++] = 0;
+	else {
+		/* odometer walk: runs along dimension 0, carries into the
+		 * outer digits (no division per element) */
+		int64_t dig[XM_MAX_DIM] = {0}, base = 0;
+		for (e = 0; e < total; e += size[0]) {
+			for (r = 0; r < size[0]; r++)
+				p->v[p->n++] = (int32_t)(base + r * stride[0]);
+			for (d = 1; d < nd; d++) {
+				base += stride[d];
+				if (++dig[d] < size[d])
+					break;
+				base -= stride[d] * size[d];
+				dig[d] = 0;
+			}
 		}
-		p->v[p->n++] = (int32_t)o;
 	}
 	xmg_hmap_put(&p->index, h, (uint64_t)p->ndesc);
 	return p->desc[p->ndesc++].off;
