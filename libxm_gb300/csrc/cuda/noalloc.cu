@@ -139,7 +139,7 @@ using namespace xmg;
 extern "C" int
 xmgd_noalloc_begin(void)
 {
-	noalloc_scratch *sc;
+	noalloc_scratch *sc = NULL;
 	int st;
 
 	if ((st = xmgd_init()) != XMG_OK || (st = scratch_addr(&sc)) != XMG_OK)
@@ -154,7 +154,7 @@ extern "C" int
 xmgd_noalloc_dot_batch(int dtype, const xmgd_ptask_t *tasks,
     const int64_t *first, int ntasks)
 {
-	noalloc_scratch *sc;
+	noalloc_scratch *sc = NULL;
 	int st;
 
 	if (ntasks <= 0)
@@ -188,7 +188,7 @@ xmgd_noalloc_dot_batch(int dtype, const xmgd_ptask_t *tasks,
 extern "C" int
 xmgd_noalloc_result(double out[2])
 {
-	noalloc_scratch *sc;
+	noalloc_scratch *sc = NULL;
 	int st;
 
 	if ((st = scratch_addr(&sc)) != XMG_OK)
