@@ -274,42 +274,46 @@ pow2_factor(xm_scalar_t s, int *sign, int *shift)
 
 struct cand {
 	xm_dim_t ia, ib;
+	const struct xmg_block *pa, *pb;    /* the blocks at ia, ib */
 	xm_scalar_t al;
 	uint64_t da, db;
 };
 
-static int
-same_key(const xm_tensor_t *a, const xm_tensor_t *b, const struct cand *x,
-    const struct cand *y, const xm_dim_t *aidxa, const xm_dim_t *aidxb)
+/* data handle of a nonzero block (xm_tensor_get_block_data_ptr) */
+static uint64_t
+block_data(const xm_tensor_t *t, const struct xmg_block *blk)
 {
-	struct xmg_block *pa = xmg_tensor_block(a, x->ia), *qa = xmg_tensor_block(a, y->ia);
-	struct xmg_block *pb = xmg_tensor_block(b, x->ib), *qb = xmg_tensor_block(b, y->ib);
+	return blk->type == XM_BLOCK_TYPE_CANONICAL ? blk->data :
+	    t->blocks[blk->data].data;
+}
+
+static int
+same_key(const struct cand *x, const struct cand *y, const xm_dim_t *aidxa,
+    const xm_dim_t *aidxb)
+{
 	size_t k;
 
 	if (x->da != y->da || x->db != y->db)
 		return 0;
 	for (k = 0; k < aidxa->n; k++)
-		if (pa->perm.i[aidxa->i[k]] != qa->perm.i[aidxa->i[k]])
+		if (x->pa->perm.i[aidxa->i[k]] != y->pa->perm.i[aidxa->i[k]])
 			return 0;
 	for (k = 0; k < aidxb->n; k++)
-		if (pb->perm.i[aidxb->i[k]] != qb->perm.i[aidxb->i[k]])
+		if (x->pb->perm.i[aidxb->i[k]] != y->pb->perm.i[aidxb->i[k]])
 			return 0;
 	return 1;
 }
 
 static uint64_t
-cand_hash(const xm_tensor_t *a, const xm_tensor_t *b, const struct cand *x,
-    const xm_dim_t *aidxa, const xm_dim_t *aidxb)
+cand_hash(const struct cand *x, const xm_dim_t *aidxa, const xm_dim_t *aidxb)
 {
-	struct xmg_block *pa = xmg_tensor_block(a, x->ia);
-	struct xmg_block *pb = xmg_tensor_block(b, x->ib);
 	uint64_t h = xmg_hash64(x->da) ^ (xmg_hash64(x->db) * 3);
 	size_t k;
 
 	for (k = 0; k < aidxa->n; k++)
-		h = xmg_hash64(h + pa->perm.i[aidxa->i[k]] + 1);
+		h = xmg_hash64(h + x->pa->perm.i[aidxa->i[k]] + 1);
 	for (k = 0; k < aidxb->n; k++)
-		h = xmg_hash64(h + 31 * (pb->perm.i[aidxb->i[k]] + 1));
+		h = xmg_hash64(h + 31 * (x->pb->perm.i[aidxb->i[k]] + 1));
 	return h == XMG_HMAP_EMPTY ? h - 1 : h;
 }
 
@@ -481,13 +485,15 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			bb = xmg_tensor_block(b, ib);
 			cand[i].ia = ia;
 			cand[i].ib = ib;
+			cand[i].pa = ba;
+			cand[i].pb = bb;
 			cand[i].al = 0;
 			if (ba->type != XM_BLOCK_TYPE_ZERO &&
 			    bb->type != XM_BLOCK_TYPE_ZERO) {
 				cand[i].al = xm_scalar_mul(ba->scalar,
 				    bb->scalar, c->type);
-				cand[i].da = xm_tensor_get_block_data_ptr(a, ia);
-				cand[i].db = xm_tensor_get_block_data_ptr(b, ib);
+				cand[i].da = block_data(a, ba);
+				cand[i].db = block_data(b, bb);
 			}
 			xm_dim_inc_mask(&ia, &nba, &p->cidxa);
 			xm_dim_inc_mask(&ib, &nbb, &p->cidxb);
@@ -500,10 +506,9 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			uint64_t h;
 			if (cand[i].al == 0)
 				continue;
-			h = cand_hash(a, b, &cand[i], &p->aidxa, &p->aidxb);
+			h = cand_hash(&cand[i], &p->aidxa, &p->aidxb);
 			while (xmg_hmap_get(&merge, h, &rep) &&
-			    !same_key(a, b, &cand[rep], &cand[i], &p->aidxa,
-			    &p->aidxb))
+			    !same_key(&cand[rep], &cand[i], &p->aidxa, &p->aidxb))
 				h = xmg_hash64(h + 1);	/* collision: rehash */
 			if (xmg_hmap_get(&merge, h, &rep)) {
 				cand[rep].al = xm_scalar_add(cand[rep].al,
