@@ -500,8 +500,7 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		}
 		/* merge (contract.c:180-192): first member of each class
 		 * accumulates the others' factors in index order */
-		xmg_hmap_free(&merge);
-		xmg_hmap_init(&merge);
+		xmg_hmap_clear(&merge);
 		for (i = 0; i < nblkk; i++) {
 			uint64_t h;
 			if (cand[i].al == 0)

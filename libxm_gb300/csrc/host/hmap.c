@@ -28,6 +28,14 @@ xmg_hmap_free(xmg_hmap_t *m)
 	memset(m, 0, sizeof *m);
 }
 
+void
+xmg_hmap_clear(xmg_hmap_t *m)
+{
+	if (m->cap)
+		memset(m->keys, 0xff, m->cap * sizeof(uint64_t));
+	m->len = 0;
+}
+
 static int
 grow(xmg_hmap_t *m)
 {

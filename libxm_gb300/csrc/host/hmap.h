@@ -13,6 +13,8 @@ typedef struct {
 
 void xmg_hmap_init(xmg_hmap_t *m);
 void xmg_hmap_free(xmg_hmap_t *m);
+/* Remove every entry, keeping the capacity. */
+void xmg_hmap_clear(xmg_hmap_t *m);
 /* Returns 1 and sets *val when found. */
 int xmg_hmap_get(const xmg_hmap_t *m, uint64_t key, uint64_t *val);
 /* Insert or overwrite; returns non-zero on out-of-memory. */
