@@ -78,6 +78,33 @@ def build(verbose=False):
     return LIB
 
 
+def build_sanitized(out_dir):
+    """The host sources built with AddressSanitizer and UBSan (the CUDA
+    objects as usual) into out_dir/libxmgb.so, for running the CPU test
+    suite with the sanitizer runtimes preloaded:
+
+        LD_PRELOAD="$(gcc -print-file-name=libasan.so) $(gcc -print-file-name=libubsan.so)" \
+        ASAN_OPTIONS=detect_leaks=0:verify_asan_link_order=0 python -c "
+        import libxm_gb300, pytest, sys
+        libxm_gb300.LIB_PATH = 'OUT_DIR/libxmgb.so'
+        sys.exit(pytest.main(['tests', '-q', '-m', 'not gpu']))"
+    """
+    build()
+    os.makedirs(out_dir, exist_ok=True)
+    objs = []
+    for src in sorted(glob.glob(os.path.join(CSRC, "host", "*.c"))):
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
+        cmd = ["gcc", "-O1", "-g", "-fPIC", "-std=gnu11", "-fno-omit-frame-pointer",
+               "-fsanitize=address,undefined"] + INC + ["-c", src, "-o", obj]
+        subprocess.run(cmd, check=True)
+        objs.append(obj)
+    objs += sorted(glob.glob(os.path.join(OBJ, "*.cu.o")))
+    lib = os.path.join(out_dir, "libxmgb.so")
+    subprocess.run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + [
+        "-lcudart_static", "-ldl", "-lrt", "-lpthread", "-lm", "-lasan", "-lubsan"], check=True)
+    return lib
+
+
 def _arch_tag():
     try:
         with open(LIB + ".arch") as f:
@@ -87,4 +114,7 @@ def _arch_tag():
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    if "--sanitize" in sys.argv:
+        print(build_sanitized(sys.argv[sys.argv.index("--sanitize") + 1]))
+    else:
+        print(build(verbose="-v" in sys.argv))
