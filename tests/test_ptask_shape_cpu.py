@@ -11,8 +11,6 @@ import itertools
 import numpy as np
 import pytest
 
-from libxm_gb300 import api  # noqa: F401  (loads the library through the fixture)
-
 
 class PTask(C.Structure):
     _fields_ = [("dst", C.c_uint64), ("src", C.c_uint64),
