@@ -80,14 +80,17 @@ int xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
     const char *idxc, int policy, long long out[4]);
 
 /* The out-of-core batch plans, cut on the host without a device from the
- * whole plan for b's blocks split into nbatch equal runs (in file order):
- * out = {batches, pairs over all batches, work-list items of `policy` over
- * all batches, 1 if every pair of the whole plan is in exactly one batch,
- * in its order, with its views, the flops add up and every batch's work
- * list holds its invariants}.  For tests. */
+ * whole plan, for b's blocks (in file order) in the streamed path's
+ * batches of at most `region` bytes, or, with region <= 0, in nbatch
+ * equal runs: out = {batches, pairs over all batches, work-list items of
+ * `policy` over all batches, 1 if every block lies aligned inside its
+ * batch's region after the previous one, every pair of the whole plan is
+ * in exactly one batch, in its order, with its views, the flops add up and
+ * every batch's work list holds its invariants}.  For tests. */
 int xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, const char *idxa, const char *idxb,
-    const char *idxc, int nbatch, int policy, long long out[4]);
+    const char *idxc, int nbatch, long long region, int policy,
+    long long out[4]);
 
 /* Statistics of the last xm_contract / xmg_contract on this process. */
 typedef struct {

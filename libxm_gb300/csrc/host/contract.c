@@ -1058,6 +1058,39 @@ distinct_b(const plan_t *p, struct hsz **out)
 	return nu;
 }
 
+/* b's blocks (distinct, in file order) in batches of at most `region`
+ * bytes, each block at a STAGE_ALIGN-aligned offset of its batch: batch k
+ * holds blocks bstart[k] .. bstart[k + 1] - 1 (bstart[nb] = nu), block i
+ * at offset off[i]; *rbytes is the largest batch.  A block larger than the
+ * region alone is an error. */
+static int
+form_batches(const struct hsz *u, size_t nu, size_t region, uint64_t *off,
+    size_t *bstart, size_t *nb, uint64_t *rbytes)
+{
+	uint64_t run = 0;
+	size_t i;
+
+	*nb = 0;
+	*rbytes = 0;
+	for (i = 0; i < nu; i++) {
+		uint64_t al = (u[i].sz + STAGE_ALIGN - 1) / STAGE_ALIGN * STAGE_ALIGN;
+		if (al > region)
+			return xmg_seterr(XMG_ENOMEM, "xm_contract: a block of b "
+			    "(%llu bytes) exceeds the staging region (%zu bytes)",
+			    (unsigned long long)u[i].sz, region);
+		if (i == 0 || run + al > region) {
+			bstart[(*nb)++] = i;
+			run = 0;
+		}
+		off[i] = run;
+		run += al;
+		if (run > *rbytes)
+			*rbytes = run;
+	}
+	bstart[*nb] = nu;
+	return XMG_OK;
+}
+
 static int
 batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
     struct batch_buf *bb, xm_scalar_t alpha, xm_scalar_t beta, int prec,
@@ -1156,7 +1189,8 @@ same_pair(const xmgd_pair_t *x, const xmgd_pair_t *y)
 int
 xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, const char *idxa, const char *idxb,
-    const char *idxc, int nbatch, int policy, long long out[4])
+    const char *idxc, int nbatch, long long region, int policy,
+    long long out[4])
 {
 	plan_t p;
 	struct batch_buf bb;
@@ -1166,11 +1200,12 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 	unsigned char *used = NULL;
 	double flops = 0;
 	long long wl[4], npairs = 0, items = 0;
-	size_t nu, i, k;
+	uint64_t *off = NULL, rbytes;
+	size_t nu, i, k, *bstart = NULL, nb;
 	int st, l, j, q, ok = 1;
 
 	memset(out, 0, 4 * sizeof *out);
-	if (nbatch < 1)
+	if (region <= 0 && nbatch < 1)
 		return xmg_seterr(XMG_EINVAL, "xmg_batch_plan_check: nbatch < 1");
 	init_plan(&p);
 	p.collect = 1;
@@ -1181,14 +1216,39 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 	}
 	nu = distinct_b(&p, &u);
 	batch_buf_alloc(&bb, &p);
-	if ((used = calloc(p.npr + 1, 1)) == NULL)
+	used = calloc(p.npr + 1, 1);
+	off = malloc((nu + 1) * sizeof *off);
+	bstart = malloc((nu + (size_t)(nbatch > 0 ? nbatch : 0) + 2) *
+	    sizeof *bstart);
+	if (!used || !off || !bstart)
 		xm_fatal("%s: out of memory", __func__);
+	if (region > 0) {
+		/* the streamed path's batches of at most `region` bytes: each
+		 * block inside the region, aligned, after the previous one */
+		if ((st = form_batches(u, nu, (size_t)region, off, bstart, &nb,
+		    &rbytes)) != XMG_OK)
+			goto done;
+		if (nu > 0 && (bstart[0] != 0 || bstart[nb] != nu ||
+		    rbytes > (uint64_t)region))
+			ok = 0;
+		for (k = 0; k < nb; k++)
+			for (i = bstart[k]; i < bstart[k + 1]; i++)
+				if (off[i] % STAGE_ALIGN != 0 ||
+				    off[i] + u[i].sz > (uint64_t)region ||
+				    (i > bstart[k] && off[i] < off[i - 1] + u[i - 1].sz) ||
+				    (i == bstart[k] && off[i] != 0))
+					ok = 0;
+	} else {
+		/* nbatch equal runs of b's blocks */
+		nb = (size_t)nbatch;
+		for (k = 0; k <= nb; k++)
+			bstart[k] = nu * k / nb;
+	}
 	xmg_hmap_init(&dmap);
-	for (k = 0; k < (size_t)nbatch && st == XMG_OK; k++) {
-		/* batch k: the k-th of nbatch equal runs of b's blocks */
+	for (k = 0; k < nb && st == XMG_OK; k++) {
 		xmg_hmap_free(&dmap);
 		xmg_hmap_init(&dmap);
-		for (i = nu * k / nbatch; i < nu * (k + 1) / nbatch; i++)
+		for (i = bstart[k]; i < bstart[k + 1]; i++)
 			if (xmg_hmap_put(&dmap, u[i].h, u[i].h))
 				xm_fatal("%s: out of memory", __func__);
 		if ((st = batch_plan(&p, &dmap, NULL, &bb, 1, k == 0 ? 0 : 1,
@@ -1238,12 +1298,15 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 				ok = 0;
 		if (npairs != p.npr || flops != p.flops)
 			ok = 0;
-		out[0] = nbatch;
+		out[0] = (long long)nb;
 		out[1] = npairs;
 		out[2] = items;
 		out[3] = ok;
 	}
 	xmg_hmap_free(&dmap);
+done:
+	free(off);
+	free(bstart);
 	free(used);
 	free(u);
 	batch_buf_free(&bb);
@@ -1269,7 +1332,7 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	uint64_t *VH = NULL, *VSZ = NULL, *VD = NULL, *JH = NULL, *JSZ = NULL,
 	    *JD = NULL;
 	size_t nv = 0;
-	uint64_t reg[2] = {0, 0}, rbytes = 0, run;
+	uint64_t reg[2] = {0, 0}, rbytes = 0;
 	size_t budget, region, nu = 0, i, *bstart = NULL, nb = 0, k;
 	struct io_job io[2];
 	xmg_hmap_t filt;
@@ -1319,27 +1382,13 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 	bstart = malloc((nu + 1) * sizeof *bstart);
 	if (!H || !SZ || !OFF || !D || !bstart)
 		xm_fatal("%s: out of memory", __func__);
-	run = 0;
 	for (i = 0; i < nu; i++) {
-		uint64_t al = (u[i].sz + STAGE_ALIGN - 1) / STAGE_ALIGN * STAGE_ALIGN;
-		if (al > region) {
-			*st = xmg_seterr(XMG_ENOMEM, "xm_contract: a block of b "
-			    "(%llu bytes) exceeds the staging region (%zu bytes)",
-			    (unsigned long long)u[i].sz, region);
-			goto out;
-		}
-		if (i == 0 || run + al > region) {
-			bstart[nb++] = i;
-			run = 0;
-		}
 		H[i] = u[i].h;
 		SZ[i] = u[i].sz;
-		OFF[i] = run;
-		run += al;
-		if (run > rbytes)
-			rbytes = run;
 	}
-	bstart[nb] = nu;
+	if ((*st = form_batches(u, nu, region, OFF, bstart, &nb, &rbytes)) !=
+	    XMG_OK)
+		goto out;
 	memset(io, 0, sizeof io);
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;

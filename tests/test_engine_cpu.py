@@ -261,10 +261,13 @@ def test_gemm_work_lists_hold_their_invariants(engine, pagefile, name):
                                          ("cfg3", 5), ("cfg5", 3)])
 def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbatch):
     """The out-of-core path builds the whole plan once and cuts each batch's
-    plan from it.  Cut on the host for b's blocks in nbatch runs: every
-    merged pair lands in exactly one batch, in its output block's order,
-    with its views and tables; the flops add up to the whole plan's; every
-    batch's stacked work list holds the kernel's invariants."""
+    plan from it.  Cut on the host for b's blocks in nbatch runs, and in the
+    streamed path's own batches of at most a region's bytes: every merged
+    pair lands in exactly one batch, in its output block's order, with its
+    views and tables; the flops add up to the whole plan's; every batch's
+    stacked work list holds the kernel's invariants; every block lies
+    aligned inside its batch's region; a block larger than the region is
+    refused."""
     gen = {"cfg2": lambda: W.cfg2(engine, pagefile),
            "cfg3": lambda: W.cfg3(engine, pagefile, dtype=api.DOUBLE_COMPLEX),
            "cfg5": lambda: W.cfg5(engine, pagefile, v_blocks=8)}[name]
@@ -277,7 +280,7 @@ def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbat
     try:
         args = (w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
         out = (api.C.c_longlong * 4)()
-        engine.check(engine.xmg_batch_plan_check(*args, nbatch, 6, out))
+        engine.check(engine.xmg_batch_plan_check(*args, nbatch, 0, 6, out))
         batches, npairs, items, ok = list(out)
         assert ok == 1 and batches == nbatch
         whole = _work_list(engine, w, 6)
@@ -290,7 +293,16 @@ def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbat
         else:
             assert items >= whole[0]
         with pytest.raises(api.XmError):
-            engine.check(engine.xmg_batch_plan_check(*args, 0, 6, out))
+            engine.check(engine.xmg_batch_plan_check(*args, 0, 0, 6, out))
+        sizes = [engine.xm_tensor_get_block_bytes(w.b.h, api.Dim.of(blk))
+                 for blk in w.b.canonical_blocks()]
+        for parts in (1, nbatch + 1):
+            region = sum(sizes) // parts + 256 * len(sizes)
+            engine.check(engine.xmg_batch_plan_check(*args, 0, region, 6, out))
+            assert out[3] == 1 and out[1] == npairs
+            assert out[0] > 1 if parts > 1 else out[0] == 1
+        with pytest.raises(api.XmError):
+            engine.check(engine.xmg_batch_plan_check(*args, 0, max(sizes) - 1, 6, out))
     finally:
         for t in w.tensors():
             t.free(data=True)
@@ -313,7 +325,7 @@ def test_plan_checks_on_reference_cases(engine, pagefile, ci):
                 assert out[3] == 1, (dt, pol)
             npairs = len(H.pair_structure_engine(engine, a, b, c, ia, ib, ic))
             for nbatch in (1, 2, 5):
-                engine.check(engine.xmg_batch_plan_check(*args, nbatch, 6, out))
+                engine.check(engine.xmg_batch_plan_check(*args, nbatch, 0, 6, out))
                 assert out[3] == 1 and out[1] == npairs, (dt, nbatch)
         finally:
             for t in (a, b, c):
