@@ -87,3 +87,44 @@ def test_pagefile_handles_match_reference(engine, reference, seed):
         ed.xm_allocator_destroy(ea)
         rd.xm_allocator_destroy(ra)
         os.rmdir(d)
+
+
+def _describe(t):
+    """Everything the tensor layer exposes about a tensor's blocks."""
+    out = {"canonical": t.canonical_blocks()}
+    nb = t.nblocks()
+    blocks = []
+    for idx in np.ndindex(*nb):
+        typ = t.block_type(idx)
+        row = (idx, typ, tuple(t.block_dims(idx)))
+        if typ != 0:      # XM_BLOCK_TYPE_ZERO
+            row += (tuple(t.block_perm(idx)), complex(t.block_scalar(idx)), t.data_ptr(idx))
+        blocks.append(row)
+    out["blocks"] = blocks
+    return out
+
+
+@pytest.mark.parametrize("ci", range(46))
+def test_tensor_layer_matches_reference(engine, reference, ci):
+    """The reference test driver's tensors built through both libraries on
+    pagefile allocators: canonical block lists, block types, dimensions,
+    permutations, scalars and data handles are identical."""
+    import cases
+    from libxm_gb300 import api
+    make = cases.CONTRACT_TESTS[ci][0]
+    d = tempfile.mkdtemp()
+    ea = api.Allocator(engine, os.path.join(d, "engine"))
+    ra = api.Allocator(reference, os.path.join(d, "reference"))
+    try:
+        for dt in (api.FLOAT, api.FLOAT_COMPLEX, api.DOUBLE, api.DOUBLE_COMPLEX):
+            et, rt = make(engine, ea, dt), make(reference, ra, dt)
+            try:
+                for x, y in zip(et, rt):
+                    assert _describe(x) == _describe(y), (ci, dt)
+            finally:
+                for t in et + rt:
+                    t.free()
+    finally:
+        ea.destroy()
+        ra.destroy()
+        os.rmdir(d)
