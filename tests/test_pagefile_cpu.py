@@ -1,9 +1,12 @@
-"""The pagefile allocator (alloc.c:40-145, 252-300 of the reference): the
-same data handles as the reference's own allocator for the same sequence
-of allocations and releases (first-fit page runs, file growth, handle =
-page offset | pages << 32), and the bytes written through one handle read
-back unchanged while every other live handle is written too.  Host only:
-no device memory is involved."""
+"""Host layers checked against the reference library compiled from its own
+sources (skipped where its checkout is absent).  The pagefile allocator
+(alloc.c:40-145, 252-300): the same data handles as the reference's own
+allocator for the same sequence of allocations and releases (first-fit
+page runs, file growth, handle = page offset | pages << 32), and the bytes
+written through one handle read back unchanged while every other live
+handle is written too.  The tensor layer (tensor.c:26-336): the reference
+test driver's tensors have the same blocks, permutations, scalars and
+data handles.  No device memory is involved."""
 import ctypes as C
 import os
 import tempfile
