@@ -279,6 +279,24 @@ struct cand {
 	uint64_t da, db;
 };
 
+/* xm_dim_inc_mask that also advances the index's linear position in the
+ * block grid (st: the grid's strides, index 0 fastest) */
+static size_t
+inc_mask_linear(xm_dim_t *idx, const xm_dim_t *dim, const xm_dim_t *mask,
+    const size_t *st, size_t lin)
+{
+	size_t k, pos;
+
+	for (k = 0; k < mask->n; k++) {
+		pos = mask->i[k];
+		if (++idx->i[pos] < dim->i[pos])
+			return lin + st[pos];
+		lin -= (dim->i[pos] - 1) * st[pos];
+		idx->i[pos] = 0;
+	}
+	return lin;
+}
+
 /* data handle of a nonzero block (xm_tensor_get_block_data_ptr) */
 static uint64_t
 block_data(const xm_tensor_t *t, const struct xmg_block *blk)
@@ -432,7 +450,7 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	 * 2 the full structure with data handles in place of device
 	 * addresses (no device needed: work-list checks) */
 	xm_dim_t *list, nba, nbb, blkc, ia, ib, dims, dA, dB, ka, kb;
-	size_t nlist, nblkk, l, i;
+	size_t nlist, nblkk, l, i, la, lb, sta[XM_MAX_DIM], stb[XM_MAX_DIM];
 	struct cand *cand = NULL;
 	xmg_hmap_t merge;
 	int64_t sa[XM_MAX_DIM], sb[XM_MAX_DIM], sc[XM_MAX_DIM];
@@ -448,6 +466,10 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	nba = xm_block_space_get_nblocks(a->bs);
 	nbb = xm_block_space_get_nblocks(b->bs);
 	nblkk = xm_dim_dot_mask(&nba, &p->cidxa);
+	for (l = 0, sta[0] = stb[0] = 1; l + 1 < XM_MAX_DIM; l++) {
+		sta[l + 1] = sta[l] * (l < nba.n ? nba.i[l] : 1);
+		stb[l + 1] = stb[l] * (l < nbb.n ? nbb.i[l] : 1);
+	}
 	xm_tensor_get_canonical_block_list(c, &list, &nlist);
 	if (nblkk > 0 && (cand = malloc(nblkk * sizeof *cand)) == NULL)
 		xm_fatal("%s: out of memory", __func__);
@@ -480,9 +502,11 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		ib = xm_dim_zero(nbb.n);
 		xm_dim_set_mask(&ia, &p->aidxa, &blkc, &p->cidxc);
 		xm_dim_set_mask(&ib, &p->aidxb, &blkc, &p->aidxc);
+		la = xmg_tensor_block_linear(a, ia);
+		lb = xmg_tensor_block_linear(b, ib);
 		for (i = 0; i < nblkk; i++) {
-			ba = xmg_tensor_block(a, ia);
-			bb = xmg_tensor_block(b, ib);
+			ba = &a->blocks[la];
+			bb = &b->blocks[lb];
 			cand[i].ia = ia;
 			cand[i].ib = ib;
 			cand[i].pa = ba;
@@ -495,8 +519,8 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 				cand[i].da = block_data(a, ba);
 				cand[i].db = block_data(b, bb);
 			}
-			xm_dim_inc_mask(&ia, &nba, &p->cidxa);
-			xm_dim_inc_mask(&ib, &nbb, &p->cidxb);
+			la = inc_mask_linear(&ia, &nba, &p->cidxa, sta, la);
+			lb = inc_mask_linear(&ib, &nbb, &p->cidxb, stb, lb);
 		}
 		/* merge (contract.c:180-192): first member of each class
 		 * accumulates the others' factors in index order */
