@@ -72,6 +72,7 @@ typedef struct {
 		int32_t off;
 	} *desc;
 	int ndesc, capdesc;
+	int overflow;            /* the pool outgrew int32 offsets */
 } tabpool_t;
 
 /* Offset table sum_d digit_d(e) * stride[d] (first dimension fastest),
@@ -102,6 +103,10 @@ tab_intern(tabpool_t *p, int nd, const int64_t *size, const int64_t *stride)
 		    memcmp(t->stride, stride, (size_t)nd * sizeof *stride) == 0)
 			return t->off;
 		h = xmg_hash64(h + 1);	/* collision: probe another key */
+	}
+	if (p->n + total > INT32_MAX) {
+		p->overflow = 1;	/* the planner reports it */
+		return 0;
 	}
 	while (p->n + total > p->cap) {
 		p->cap = p->cap ? 2 * p->cap : 4096;
@@ -477,6 +482,12 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	for (l = 0; l < nlist && st == XMG_OK; l++) {
 		blkc = list[l];
 		dims = xm_block_space_get_block_dims(c->bs, blkc);
+		/* offsets inside a block are int32 on the device */
+		if (xm_dim_dot(&dims) > INT32_MAX) {
+			st = xmg_seterr(XMG_EINVAL, "xm_contract: a block of c has "
+			    "more than 2^31 - 1 elements");
+			break;
+		}
 		GROW(p->cb, p->ncb, p->capcb);
 		GROW(p->emulatable, p->ncb, p->capem);
 		cb = &p->cb[p->ncb];
@@ -557,6 +568,11 @@ build_plan(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 			}
 			dA = xm_block_space_get_block_dims(a->bs, cand[i].ia);
 			dB = xm_block_space_get_block_dims(b->bs, cand[i].ib);
+			if (xm_dim_dot(&dA) > INT32_MAX || xm_dim_dot(&dB) > INT32_MAX) {
+				st = xmg_seterr(XMG_EINVAL, "xm_contract: a block of a "
+				    "or b has more than 2^31 - 1 elements");
+				break;
+			}
 			GROW(p->pr, p->npr, p->cappr);
 			pr = &p->pr[p->npr++];
 			memset(pr, 0, sizeof *pr);
@@ -611,6 +627,9 @@ next:
 	xmg_hmap_free(&merge);
 	free(cand);
 	free(list);
+	if (st == XMG_OK && p->tabs.overflow)
+		st = xmg_seterr(XMG_EINVAL, "xm_contract: the contraction's "
+		    "offset tables exceed 2^31 - 1 entries");
 	return st;
 }
 

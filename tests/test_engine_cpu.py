@@ -330,3 +330,28 @@ def test_plan_checks_on_reference_cases(engine, pagefile, ci):
         finally:
             for t in (a, b, c):
                 t.free()
+
+
+def test_blocks_beyond_int32_offsets_are_refused(engine, pagefile):
+    """Offsets inside a block are 32-bit on the device: the planner refuses
+    a block with more than 2^31 - 1 elements with an error instead of
+    building wrapped offset tables.  Blocks are set with placeholder data
+    handles (nothing is allocated or read)."""
+    set_raw = engine.dll.xm_tensor_set_canonical_block_raw
+    set_raw.argtypes = [api.C.c_void_p, api.Dim, api.C.c_uint64]
+    set_raw.restype = None
+    big, small = 50000, 8            # 50000^2 = 2.5e9 elements > 2^31 - 1
+    for da, db, dc, ia, ib, ic in (([big, big], [big, small], [big, small], "ij", "jk", "ik"),
+                                   ([big, small], [small, big], [big, big], "ik", "kj", "ij")):
+        spaces = [api.BlockSpace(engine, d) for d in (da, db, dc)]
+        ts = [api.Tensor(engine, s, api.DOUBLE, pagefile) for s in spaces]
+        for n, t in enumerate(ts):
+            set_raw(t.h, api.Dim.of([0, 0]), 4096 * (n + 1))
+        f = engine.xmg_contract_flops(ts[0].h, ts[1].h, ts[2].h, ia.encode(), ib.encode(),
+                                      ic.encode())
+        assert f == -1
+        assert "2^31" in engine.xmg_last_error().decode()
+        for t in ts:
+            t.free(data=False)
+        for s in spaces:
+            s.free()
