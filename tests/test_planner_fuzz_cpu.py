@@ -5,8 +5,10 @@ and (anti)symmetric dimensions stored as derivative blocks with a +-1
 scalar: a transposition of two dimensions, or the exchange of two pairs of
 dimensions at once.  The engine's merged pair list
 (output block, merged factor, m, n, k) and its flop count must equal the
-oracle's bit for bit (contract.c:161-218 of the reference).  No device is
-involved: the engine plans on a pagefile allocator."""
+oracle's bit for bit (contract.c:161-218 of the reference), and the
+split-precision GEMM's work lists and the out-of-core batch plans built
+from it hold their invariants.  No device is involved: the engine plans on
+a pagefile allocator.  The scalar type cycles over the four kinds."""
 import itertools
 import os
 import tempfile
@@ -89,12 +91,12 @@ def _layout(rng, defs, idx, contracted):
     return kinds
 
 
-def _build(lib, alloc, defs, idx, kinds):
+def _build(lib, alloc, defs, idx, kinds, dtype):
     bs = api.BlockSpace(lib, [defs[x][0] for x in idx])
     for d, x in enumerate(idx):
         for c in defs[x][1]:
             bs.split(d, c)
-    t = api.Tensor(lib, bs, api.DOUBLE, alloc)
+    t = api.Tensor(lib, bs, dtype, alloc)
     bs.free()
     for blk, k in kinds.items():
         if k[0] == "c":
@@ -110,9 +112,10 @@ def test_random_contractions_plan_like_the_oracle(engine, oracle, pagefile, seed
     rng = np.random.default_rng(1000 + seed)
     defs, idxa, idxb, idxc, ks = _case(rng)
     kinds = [_layout(rng, defs, s, ks) for s in (idxa, idxb, idxc)]
+    dt = (api.DOUBLE, api.DOUBLE_COMPLEX, api.FLOAT, api.FLOAT_COMPLEX)[seed % 4]
     oal = api.Allocator(oracle)
-    et = [_build(engine, pagefile, defs, s, k) for s, k in zip((idxa, idxb, idxc), kinds)]
-    ot = [_build(oracle, oal, defs, s, k) for s, k in zip((idxa, idxb, idxc), kinds)]
+    et = [_build(engine, pagefile, defs, s, k, dt) for s, k in zip((idxa, idxb, idxc), kinds)]
+    ot = [_build(oracle, oal, defs, s, k, dt) for s, k in zip((idxa, idxb, idxc), kinds)]
     try:
         for t in ot:
             H.fill_random(t, rng)
@@ -121,7 +124,17 @@ def test_random_contractions_plan_like_the_oracle(engine, oracle, pagefile, seed
         assert mine == ref, (idxa, idxb, idxc, defs)
         flops = engine.xmg_contract_flops(et[0].h, et[1].h, et[2].h, idxa.encode(),
                                           idxb.encode(), idxc.encode())
-        assert flops == sum(2 * m * n * k for _, _, m, n, k in ref)
+        mult = 8 if dt in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX) else 2
+        assert flops == sum(mult * m * n * k for _, _, m, n, k in ref)
+        # the split-precision work lists and the out-of-core batch cut
+        args = (et[0].h, et[1].h, et[2].h, idxa.encode(), idxb.encode(), idxc.encode())
+        out = (api.C.c_longlong * 4)()
+        for pol in (0, 1, 2, 6):
+            engine.check(engine.xmg_work_list_check(*args, pol, out))
+            assert out[3] == 1, pol
+        for nbatch in (1, 3):
+            engine.check(engine.xmg_batch_plan_check(*args, nbatch, 0, 6, out))
+            assert out[3] == 1 and out[1] == len(mine), nbatch
     finally:
         for t in et + ot:
             t.free()
