@@ -79,9 +79,10 @@ def build(verbose=False):
 
 
 def build_sanitized(out_dir):
-    """The host sources built with AddressSanitizer and UBSan (the CUDA
-    objects as usual) into out_dir/libxmgb.so, for running the CPU test
-    suite with the sanitizer runtimes preloaded:
+    """The library with its host code (the C sources and the host side of
+    the CUDA sources) built with AddressSanitizer and UBSan into
+    out_dir/libxmgb.so, for running the CPU test suite with the sanitizer
+    runtimes preloaded:
 
         LD_PRELOAD="$(gcc -print-file-name=libasan.so) $(gcc -print-file-name=libubsan.so)" \
         ASAN_OPTIONS=detect_leaks=0:verify_asan_link_order=0 python -c "
@@ -89,16 +90,24 @@ def build_sanitized(out_dir):
         libxm_gb300.LIB_PATH = 'OUT_DIR/libxmgb.so'
         sys.exit(pytest.main(['tests', '-q', '-m', 'not gpu']))"
     """
-    build()
     os.makedirs(out_dir, exist_ok=True)
-    objs = []
+    san = ["-fsanitize=address", "-fsanitize=undefined", "-fno-omit-frame-pointer"]
+    cmds = []
     for src in sorted(glob.glob(os.path.join(CSRC, "host", "*.c"))):
         obj = os.path.join(out_dir, os.path.basename(src) + ".o")
-        cmd = ["gcc", "-O1", "-g", "-fPIC", "-std=gnu11", "-fno-omit-frame-pointer",
-               "-fsanitize=address,undefined"] + INC + ["-c", src, "-o", obj]
-        subprocess.run(cmd, check=True)
-        objs.append(obj)
-    objs += sorted(glob.glob(os.path.join(OBJ, "*.cu.o")))
+        cmds.append(["gcc", "-O1", "-g", "-fPIC", "-std=gnu11"] + san + INC +
+                    ["-c", src, "-o", obj])
+    for src in sorted(glob.glob(os.path.join(CSRC, "cuda", "*.cu"))):
+        # the host side of the CUDA sources (plans, work lists) too
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
+        cmds.append([NVCC, "-O1", "-g", "-std=c++17", "--expt-relaxed-constexpr",
+                     "-Xcompiler", "-fPIC"] + [x for f in san for x in ("-Xcompiler", f)] +
+                    ARCH + INC + ["-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        for r in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds):
+            if r.returncode != 0:
+                raise RuntimeError("compile failed: %s\n%s" % (" ".join(r.args), r.stderr))
+    objs = [c[c.index("-o") + 1] for c in cmds]
     lib = os.path.join(out_dir, "libxmgb.so")
     subprocess.run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + [
         "-lcudart_static", "-ldl", "-lrt", "-lpthread", "-lm", "-lasan", "-lubsan"], check=True)
