@@ -1,0 +1,66 @@
+"""Error behaviour of xm_contract against the reference library compiled
+from its own sources: for each invalid call of the reference's validation
+(contract.c:237-280) both libraries print the same `libxm: ...` line and
+exit with status 1.  Each call runs in a child process (the public API
+exits on error, util.c:24-35); validation precedes any device use, so no
+GPU is involved."""
+import os
+import subprocess
+import sys
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CHILD = r'''
+import os, sys
+sys.path.insert(0, {root!r})
+from libxm_gb300 import api
+lib = api.Lib({path!r})
+d = {tmp!r}
+al = api.Allocator(lib, os.path.join(d, "pf"))
+al2 = api.Allocator(lib, os.path.join(d, "pf2"))
+
+def space(dims, cuts):
+    bs = api.BlockSpace(lib, dims)
+    for k, c in enumerate(cuts):
+        if c:
+            bs.split(k, c)
+    return bs
+
+def tensor(dims, cuts, dtype=api.DOUBLE, alloc=al):
+    return api.Tensor(lib, space(dims, cuts), dtype, alloc)
+
+case = {case!r}
+a = tensor([6, 8], [3, 4], api.FLOAT if case == "type" else api.DOUBLE)
+b = tensor([8, 5], [5 if case == "ab" else 4, 2], alloc=al2 if case == "alloc" else al)
+c = tensor([6, 5], [2 if case == "ac" else 3, 3 if case == "bc" else 2])
+idx = {{"length": ("ik", "kj", "ijj"),
+       "letters": ("ik", "kj", "ix")}}.get(case, ("ik", "kj", "ij"))
+sys.stderr.flush()
+lib.xm_contract(api.Scalar.of(1), a.h, b.h, api.Scalar.of(0), c.h,
+                idx[0].encode(), idx[1].encode(), idx[2].encode())
+print("returned")
+'''
+
+CASES = ["length", "letters", "type", "alloc", "ab", "ac", "bc"]
+
+
+def _run(path, case):
+    # the child exits through the error path, so its pagefiles go with the
+    # directory
+    with tempfile.TemporaryDirectory() as tmp:
+        r = subprocess.run([sys.executable, "-c",
+                            CHILD.format(root=ROOT, path=path, case=case, tmp=tmp)],
+                           capture_output=True, text=True, timeout=120)
+    lines = [l for l in r.stderr.splitlines() if l.startswith("libxm:")]
+    return r.returncode, lines
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_contract_errors_match_reference(engine, reference, case):
+    mine = _run(engine.path, case)
+    ref = _run(reference.path, case)
+    assert ref[0] == 1 and ref[1], ref
+    assert mine == ref
