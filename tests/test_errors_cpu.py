@@ -1,7 +1,8 @@
 """Error behaviour against the reference library compiled from its own
 sources: for each invalid call of the reference's validation in
 xm_contract (contract.c:237-280) and in xm_add / xm_copy / xm_mul /
-xm_div / xm_dot (xm.c:70-95, 165-190, 257-282, 340-365, 422-446) both
+xm_div / xm_dot (xm.c:70-95, 165-190, 257-282, 340-365, 422-446) and in
+the tensor layer's block setters, reads and writes (tensor.c:255-366) both
 libraries print the same `libxm: ...` line and exit with status 1.  Each call runs in a child process (the public API
 exits on error, util.c:24-35); validation precedes any device use, so no
 GPU is involved."""
@@ -116,6 +117,53 @@ def test_elementwise_errors_match_reference(engine, reference, fn, case):
         with tempfile.TemporaryDirectory() as tmp:
             r = subprocess.run([sys.executable, "-c", PAIR_CHILD.format(
                 root=ROOT, path=path, tmp=tmp, fn=fn, case=case)],
+                capture_output=True, text=True, timeout=120)
+        return r.returncode, [l for l in r.stderr.splitlines() if l.startswith("libxm:")]
+    mine, ref = run(engine.path), run(reference.path)
+    assert ref[0] == 1 and ref[1], ref
+    assert mine == ref
+
+
+TENSOR_CHILD = r'''
+import os, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+from libxm_gb300 import api
+lib = api.Lib({path!r})
+al = api.Allocator(lib, os.path.join({tmp!r}, "pf"))
+bs = api.BlockSpace(lib, [6, 6])
+bs.split(0, 3)
+bs.split(1, 3)
+t = api.Tensor(lib, bs, api.DOUBLE, al)
+case = {case!r}
+t.set_canonical((0, 1))
+if case == "canonical_twice":
+    t.set_canonical((0, 1))
+elif case == "derivative_on_nonzero":
+    t.set_derivative((0, 1), (0, 1), [1, 0], -1.0)
+elif case == "derivative_of_zero":
+    t.set_derivative((1, 0), (1, 1), [1, 0], -1.0)
+elif case == "bad_permutation":
+    t.set_derivative((1, 0), (0, 1), [0, 0], -1.0)
+elif case == "read_zero":
+    t.read_block((1, 1))
+elif case == "write_derivative":
+    t.set_derivative((1, 0), (0, 1), [1, 0], -1.0)
+    t.write_block((1, 0), np.zeros(9))
+print("returned")
+'''
+
+TENSOR_CASES = ["canonical_twice", "derivative_on_nonzero", "derivative_of_zero",
+                "bad_permutation", "read_zero", "write_derivative"]
+
+
+@pytest.mark.parametrize("case", TENSOR_CASES)
+def test_tensor_errors_match_reference(engine, reference, case):
+    """Block setters and block reads/writes (tensor.c:255-366)."""
+    def run(path):
+        with tempfile.TemporaryDirectory() as tmp:
+            r = subprocess.run([sys.executable, "-c", TENSOR_CHILD.format(
+                root=ROOT, path=path, tmp=tmp, case=case)],
                 capture_output=True, text=True, timeout=120)
         return r.returncode, [l for l in r.stderr.splitlines() if l.startswith("libxm:")]
     mine, ref = run(engine.path), run(reference.path)
