@@ -3,9 +3,10 @@ sources: for each invalid call of the reference's validation in
 xm_contract (contract.c:237-280) and in xm_add / xm_copy / xm_mul /
 xm_div / xm_dot (xm.c:70-95, 165-190, 257-282, 340-365, 422-446) and in
 the tensor layer's block setters, reads and writes (tensor.c:255-366) both
-libraries print the same `libxm: ...` line and exit with status 1.  Each call runs in a child process (the public API
-exits on error, util.c:24-35); validation precedes any device use, so no
-GPU is involved."""
+libraries print the same `libxm: ...` line and exit with status 1.  Each
+call runs in a child process (the public API exits on error,
+util.c:24-35); validation precedes any device use, so no GPU is
+involved."""
 import os
 import subprocess
 import sys
