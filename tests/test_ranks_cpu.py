@@ -52,10 +52,11 @@ def test_two_ranks_barrier_and_max():
     assert res == [(0, 2, 3.0), (1, 2, 3.0)]
 
 
-def test_reference_arm_two_ranks_prints_once():
+def test_reference_arm_two_ranks_prints_once(tmp_path):
     """torchrun with two ranks: one JSON line, from rank 0, with the
     reference arm's keys; both ranks exit 0."""
-    env = dict(os.environ, OMP_NUM_THREADS="2")
+    # torchrun's own scratch directories go under the test's directory
+    env = dict(os.environ, OMP_NUM_THREADS="2", TMPDIR=str(tmp_path))
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
            "--nproc-per-node", "2", "--master-addr", "127.0.0.1",
            "--master-port", str(_free_port()), os.path.join(ROOT, "bench.py"),
