@@ -32,6 +32,8 @@ os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 import numpy as np  # noqa: E402
 
+from libxm_gb300 import api  # noqa: E402  (ctypes binding only)
+
 METRIC = "xm_contract TFLOP/s on 1 GB300: split-precision vs plain FP64 at rel err ≤1e-12"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
@@ -43,7 +45,6 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
     p.add_argument("--fp64-steps", type=int, default=2)
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-out-of-core", action="store_true",
                    help="skip the pagefile-streamed measurement")
@@ -151,47 +152,46 @@ def cpu_lib():
     return lib, "port"
 
 
-def cpu_baseline(w, ranks, target_s, engine_out=None):
-    """Time the CPU reference on a bounded sample of the workload's output
-    blocks: all host threads, OPENBLAS_NUM_THREADS=1 (it parallelises over
-    blocks itself)."""
-    from libxm_gb300 import api, workloads as W
+def cpu_contract_timed(w, reps):
+    """The CPU reference's whole xm_contract on w's workload (all canonical
+    output blocks): one untimed warm-up call, then `reps` timed calls.
+    All host threads, OPENBLAS_NUM_THREADS=1 (the reference parallelises
+    over output blocks itself).  Returns (seconds per call, best seconds,
+    {block: data})."""
+    api.contract(w.alpha, w.a, w.b, w.beta, w.c, w.idxa, w.idxb, w.idxc)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        api.contract(w.alpha, w.a, w.b, w.beta, w.c, w.idxa, w.idxb, w.idxc)
+        times.append(time.perf_counter() - t0)
+    return float(np.mean(times)), min(times), {blk: w.c.read_block(blk)
+                                               for blk in w.c.canonical_blocks()}
+
+
+def cpu_threads(lib):
+    n = lib.dll.xmo_num_threads() if hasattr(lib.dll, "xmo_num_threads") else 0
+    return int(os.environ.get("OMP_NUM_THREADS") or n or os.cpu_count())
+
+
+def cpu_baseline(w, flops, reps=3):
+    """The CPU reference timed on the whole workload (every canonical output
+    block), best of `reps` calls after one warm-up, on the same inputs as
+    the engine (the engine's A and B copied over)."""
+    from libxm_gb300 import workloads as W
     lib, kind = cpu_lib()
     al = api.Allocator(lib)
-    wc = make_workload(lib, al, w.scale, w.subset)
-    blocks = wc.c.canonical_blocks()
-    cost = block_costs(wc)
-
-    def run_sample(nblk):
-        chosen = set(blocks[:nblk])
-        c = wc.c.structure()
-        for blk in blocks:
-            if blk not in chosen:
-                lib.xm_tensor_set_zero_block(c.h, api.Dim.of(blk))
-        fl = sum(cost[i] for i in range(nblk))
-        t0 = time.perf_counter()
-        api.contract(wc.alpha, wc.a, wc.b, wc.beta, c, wc.idxa, wc.idxb, wc.idxc)
-        dt = time.perf_counter() - t0
-        out = {blk: c.read_block(blk) for blk in c.canonical_blocks()}
-        c.free()
-        return fl, dt, out
-
-    n = max(1, len(blocks) // 50)
-    fl, dt, _ = run_sample(n)
-    rate = fl / max(dt, 1e-6)
-    total = sum(cost)
-    want = min(total, rate * target_s)
-    acc, nblk = 0.0, 0
-    while nblk < len(blocks) and acc < want:
-        acc += cost[nblk]
-        nblk += 1
-    fl, dt, out = run_sample(nblk)
-    threads = lib.dll.xmo_num_threads() if hasattr(lib.dll, "xmo_num_threads") else os.cpu_count()
-    res = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": int(os.environ.get("OMP_NUM_THREADS", threads or os.cpu_count())),
+    wc = make_workload(lib, al, w.scale, w.subset, fill_data=False)
+    W.copy_data(w.a, wc.a)
+    W.copy_data(w.b, wc.b)
+    mean_s, best_s, out = cpu_contract_timed(wc, reps)
+    nblk = len(out)
+    res = {"value": flops / best_s / 1e12, "unit": "TFLOP/s", "cores": cpu_threads(lib),
            "kind": kind,
-           "sample": "%d of %d canonical output blocks (%.3e of %.3e useful flops), %.1f s"
-                     % (nblk, len(blocks), fl, total, dt)}
+           "sample": "%d of %d canonical output blocks (the whole xm_contract, %.3e useful "
+                     "flops), best of %d calls after one warm-up: %.2f s (mean %.2f s)"
+                     % (nblk, nblk, flops, reps, best_s, mean_s)}
     wc.free()
+    al.destroy()
     return res, out
 
 
@@ -211,13 +211,7 @@ def block_costs(w):
     # plan-only pass of the oracle on the same structure
     orc = api.Lib(ob.build_oracle())
     oal = api.Allocator(orc)
-    from libxm_gb300 import workloads as W
-    orig = W.fill
-    W.fill = lambda *x, **y: None
-    try:
-        wo = make_workload(orc, oal, w.scale, w.subset)
-    finally:
-        W.fill = orig
+    wo = make_workload(orc, oal, w.scale, w.subset, fill_data=False)
     import helpers as H
     orc.dll.xmo_set_plan_only(1)
     for l, _, m, n, k in H.pair_structure_oracle(orc, wo.a, wo.b, wo.c, wo.idxa, wo.idxb, wo.idxc):
@@ -380,13 +374,22 @@ def cfg5_subset(eng, api, W, v_blocks=12):
     return out
 
 
-def make_workload(lib, al, scale=1, subset=None):
+def make_workload(lib, al, scale=1, subset=None, fill_data=True):
     from libxm_gb300 import workloads as W
     ob, vb = (int(x) for x in subset.split(",")) if subset else (None, None)
-    w = W.cfg2(lib, al, scale=scale, o_blocks=ob, v_blocks=vb)
+    w = W.cfg2(lib, al, scale=scale, o_blocks=ob, v_blocks=vb, fill_data=fill_data)
     w.scale = scale
     w.subset = subset
     return w
+
+
+def workload_config(w, flops):
+    """The `config` object of both arms' JSON lines (identical keys and
+    values for the same workload)."""
+    return {"workload": w.name, "o": w.extra["o_sizes"], "v": w.extra["v_sizes"],
+            "z2_labels": {"o": w.extra["o_labels"], "v": w.extra["v_labels"]},
+            "contraction": "C(ijab)=A(ijcd)B(cdab)", "useful_flops": flops,
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
 
 
 # --------------------------------------------------------------- engine --
@@ -591,7 +594,7 @@ def engine_arm(args, ranks):
     cpu = None
     rel_emu_vs_cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
-        cpu, cpu_out = cpu_baseline(w, ranks, args.cpu_seconds)
+        cpu, cpu_out = cpu_baseline(w, flops)
         sub = {k: emu["out"][k] for k in cpu_out}
         rel_emu_vs_cpu = W.rel_frobenius(sub, cpu_out)
         rel_fp64_vs_cpu = W.rel_frobenius({k: fp64["out"][k] for k in cpu_out}, cpu_out)
@@ -603,15 +606,12 @@ def engine_arm(args, ranks):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (emulated: bf16 slices, fp32 exact partials, int64 accumulation)",
         "data": "synthetic (seeded splitmix64 uniform[-1,1]; inputs larger than L2)",
-        "config": {"workload": w.name, "o": w.extra["o_sizes"], "v": w.extra["v_sizes"],
-                   "z2_labels": {"o": w.extra["o_labels"], "v": w.extra["v_labels"]},
-                   "contraction": "C(ijab)=A(ijcd)B(cdab)", "useful_flops": flops,
-                   "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"},
+        "config": workload_config(w, flops),
         "fp64_plain": {"value": fp64_value, "ms_per_step": fp64["ms_per_step"],
                        "gemm_ms": fp64["gemm_ms"]},
         "speedup_vs_fp64_plain": value / fp64_value,
-        "rel_err": {"emu_vs_gpu_fp64": rel_emu_vs_fp64, "emu_vs_cpu_fp64_sample": rel_emu_vs_cpu,
-                    "gpu_fp64_vs_cpu_fp64_sample": rel_fp64_vs_cpu if cpu else None},
+        "rel_err": {"emu_vs_gpu_fp64": rel_emu_vs_fp64, "emu_vs_cpu_reference": rel_emu_vs_cpu,
+                    "gpu_fp64_vs_cpu_reference": rel_fp64_vs_cpu if cpu else None},
         "precision_used": "emu64" if emu["precision_used"] == api.PREC_EMU64 else "fp64",
         "phases_ms": {"gemm": emu["gemm_ms"], "split": emu["split_ms"]},
         "gemm_work_list": {"policy": emu["gemm_policy"],
@@ -627,58 +627,41 @@ def engine_arm(args, ranks):
 
 
 def reference_arm(args, ranks):
+    """The reference's CPU implementation of the path on the machine's host
+    cores: one step = one whole xm_contract over the workload (every
+    canonical output block), W untimed steps then K timed ones."""
     if ranks.rank != 0:
         return
-    from libxm_gb300 import api, workloads as W
     lib, kind = cpu_lib()
     al = api.Allocator(lib)
     w = make_workload(lib, al, args.scale, args.subset)
-    cost = block_costs(w)
-    blocks = w.c.canonical_blocks()
-    total = sum(cost)
-    # calibrate a per-step sample of roughly cpu-seconds / steps
-    per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
-
-    def make_c(nblk):
-        c = w.c.structure()
-        for blk in blocks[nblk:]:
-            lib.xm_tensor_set_zero_block(c.h, api.Dim.of(blk))
-        return c, sum(cost[:nblk])
-    c, fl = make_c(max(1, len(blocks) // 50))
-    t0 = time.perf_counter()
-    api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
-    rate = fl / max(time.perf_counter() - t0, 1e-6)
-    c.free()
-    acc, nblk = 0.0, 0
-    while nblk < len(blocks) and acc < rate * per_step:
-        acc += cost[nblk]
-        nblk += 1
-    c, fl = make_c(nblk)
+    flops = sum(block_costs(w))
+    nblk = len(w.c.canonical_blocks())
     for _ in range(args.warmup):
-        api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
-    t0 = time.perf_counter()
+        w.run()
+    times = []
     for _ in range(args.steps):
-        api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
-    dt = (time.perf_counter() - t0) / args.steps
-    value = fl / dt / 1e12
-    threads = os.environ.get("OMP_NUM_THREADS") or os.cpu_count()
-    sample = "%d of %d canonical output blocks (%.3e of %.3e useful flops) per step" % (
-        nblk, len(blocks), fl, total)
+        t0 = time.perf_counter()
+        w.run()
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    value = flops / dt / 1e12
+    sample = ("%d of %d canonical output blocks per step (the whole xm_contract, %.3e useful "
+              "flops); mean %.2f s, best %.2f s per call" % (nblk, nblk, flops, dt, min(times)))
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded splitmix64 uniform[-1,1])",
-        "config": {"workload": w.name, "contraction": "C(ijab)=A(ijcd)B(cdab)",
-                   "useful_flops_total": total, "parallelism": "host threads"},
+        "data": "synthetic (seeded splitmix64 uniform[-1,1]; inputs larger than L2)",
+        "config": workload_config(w, flops),
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": int(threads), "kind": kind,
-                         "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cpu_threads(lib),
+                         "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))
-    c.free()
     w.free()
+    al.destroy()
 
 
 def main():

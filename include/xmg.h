@@ -140,17 +140,21 @@ int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
  * need the value -- typically a host program whose own pool already holds
  * the GPU memory it may use (so any cudaMalloc would fail), or a solver
  * evaluating a norm every iteration of a tight loop, where the regular
- * xm_dot's first-use device allocations would stall it.  Same result as
- * xm_dot(a, b, idxa, idxb), written to *result; the tensors must live in
- * GPU memory (allocator created with path NULL).  It calls no cudaMalloc,
+ * xm_dot's first-use device allocations would stall it.  The value of
+ * xm_dot(a, b, idxa, idxb), written to *result: the same block pairing and
+ * factors, summed in another order (double types agree to rounding; float
+ * types round each block's contribution and the running sum to float as
+ * xm_dot does, and agree to float rounding).  The tensors must live in GPU
+ * memory (allocator created with path NULL).  It calls no cudaMalloc,
  * cudaFree or host allocator: its task table, per-CTA partial sums and
  * running result live in one static device array of about 270 KiB that
- * every GPU loading the library keeps until exit.  Limits: blocks of at
- * most XMG_NOALLOC_MAX_CTAS * XMG_NOALLOC_ELEMS_PER_CTA elements (larger
- * ones are rejected with XMG_EINVAL), tasks run in batches of
- * XMG_NOALLOC_MAX_TASKS.  The first call on a device looks up the array's
- * device address and should come before any stream capture.  Calls share
- * the array: calls that overlap on the GPU race.  Returns XMG_* status. */
+ * the engine's GPU holds from the engine's initialisation (the first call
+ * of this library that needs the GPU, which also looks up the array's
+ * device address) until exit.  Limits: blocks of at most
+ * XMG_NOALLOC_MAX_CTAS * XMG_NOALLOC_ELEMS_PER_CTA elements (larger ones
+ * are rejected with XMG_EINVAL), tasks run in batches of
+ * XMG_NOALLOC_MAX_TASKS.  Calls share the array: calls that overlap on
+ * the GPU race.  Returns XMG_* status (XMG_EINVAL for NULL arguments). */
 #define XMG_NOALLOC_MAX_TASKS      64
 #define XMG_NOALLOC_MAX_CTAS       16384
 #define XMG_NOALLOC_ELEMS_PER_CTA  2048
@@ -159,6 +163,9 @@ int xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b,
 
 /* Wait for all device work of the engine. */
 int xmg_synchronize(void);
+
+/* Free and total bytes of the engine's device (cudaMemGetInfo). */
+int xmg_device_memory(size_t *free_bytes, size_t *total_bytes);
 
 /* Opt-in tile-aware autosplit (no counterpart in the reference, whose
  * xm_block_space_autosplit is unchanged): every dimension is cut into about

@@ -140,6 +140,7 @@ _GB_SIGS = {
     "xmg_kernel_launches": (C.c_longlong, []),
     "xmg_host_alloc": (_P, [C.c_size_t]),
     "xmg_host_free": (None, [_P]),
+    "xmg_device_memory": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
 }
 
 

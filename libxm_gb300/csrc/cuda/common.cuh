@@ -14,6 +14,7 @@ extern "C" int xmg_seterr(int code, const char *fmt, ...);
 namespace xmg {
 
 cudaStream_t stream();          /* engine compute stream */
+int device();                   /* engine device ordinal */
 int num_sms();
 int check(cudaError_t e, const char *what);
 extern long long g_launches;     /* kernels launched by the engine */

@@ -11,12 +11,15 @@
  * file-scope array below, sized once at load time.
  *
  * The array's name is only a host-side stand-in for the device object, so
- * its device address is fetched with cudaGetSymbolAddress on the first
- * call on each device, with that device current.  That first call should
- * come before any stream capture.  All calls share the one array and it
- * keeps the previous call's contents: the result is cleared at the start
- * of every call, and calls that overlap on the GPU (several host threads,
- * or several processes' streams on one context) race on it.
+ * its device address is fetched with cudaGetSymbolAddress, with the
+ * engine's device current, when the engine initialises on that device
+ * (xmgd_init calls xmgd_noalloc_setup).  That lookup also loads this
+ * file's module, which is when the driver places the array in device
+ * memory: with lazy module loading a lookup deferred to the first
+ * xmg_dot_noalloc would allocate at that call.  All calls share the one
+ * array and it keeps the previous call's contents: the result is cleared
+ * at the start of every call, and calls that overlap on the GPU (several
+ * host threads, or several processes' streams on one context) race on it.
  */
 #include <stdint.h>
 
@@ -94,9 +97,11 @@ noalloc_dot_kernel(noalloc_scratch *sc, int ntasks)
 }
 
 /* result += sum over tasks of factor_t * (sum of the task's partials), in
- * task order (deterministic) */
+ * task order (deterministic).  For float types the scaled task sum and the
+ * running result are rounded to float after every task, as xm_dot rounds
+ * each block's contribution and its running sum to the tensor's type. */
 __global__ void
-noalloc_reduce_kernel(noalloc_scratch *sc, int ntasks)
+noalloc_reduce_kernel(noalloc_scratch *sc, int ntasks, int narrow)
 {
 	if (threadIdx.x != 0 || blockIdx.x != 0)
 		return;
@@ -108,23 +113,34 @@ noalloc_reduce_kernel(noalloc_scratch *sc, int ntasks)
 			b += sc->partial[2 * c + 1];
 		}
 		const double *f = sc->tasks[k].alpha;
-		rr += f[0] * a - f[1] * b;
-		ri += f[0] * b + f[1] * a;
+		double pr = f[0] * a - f[1] * b, pi = f[0] * b + f[1] * a;
+		if (narrow) {
+			pr = (float)pr;
+			pi = (float)pi;
+			rr = (float)(rr + pr);
+			ri = (float)(ri + pi);
+		} else {
+			rr += pr;
+			ri += pi;
+		}
 	}
 	sc->result[0] = rr;
 	sc->result[1] = ri;
 }
 
+/* The array's device address on the engine's device (the one every copy
+ * and launch below goes to, whichever host thread calls); looked up with
+ * that device current. */
 static int
 scratch_addr(noalloc_scratch **out)
 {
-	int dev = 0;
+	const int dev = device();
 
-	XMG_CK(cudaGetDevice(&dev));
 	if (dev < 0 || dev >= NA_MAX_DEVICES)
 		return xmg_seterr(XMG_EINVAL, "xmg_dot_noalloc: device %d", dev);
 	if (g_addr[dev] == nullptr) {
 		void *p = nullptr;
+		XMG_CK(cudaSetDevice(dev));
 		XMG_CK(cudaGetSymbolAddress(&p, g_noalloc));
 		g_addr[dev] = static_cast<noalloc_scratch *>(p);
 	}
@@ -135,6 +151,15 @@ scratch_addr(noalloc_scratch **out)
 } /* namespace xmg */
 
 using namespace xmg;
+
+/* Called once by xmgd_init, after it made the engine's device current. */
+extern "C" int
+xmgd_noalloc_setup(void)
+{
+	noalloc_scratch *sc = NULL;
+
+	return scratch_addr(&sc);
+}
 
 extern "C" int
 xmgd_noalloc_begin(void)
@@ -177,7 +202,7 @@ xmgd_noalloc_dot_batch(int dtype, const xmgd_ptask_t *tasks,
 	default: return xmg_seterr(XMG_EINVAL, "xmg_dot_noalloc: scalar type");
 	}
 	XMG_CK(cudaGetLastError());
-	noalloc_reduce_kernel<<<1, 32, 0, stream()>>>(sc, ntasks);
+	noalloc_reduce_kernel<<<1, 32, 0, stream()>>>(sc, ntasks, dtype < 2);
 	XMG_CK(cudaGetLastError());
 	g_launches += 2;
 	/* the host task array may be reused by the caller right away */

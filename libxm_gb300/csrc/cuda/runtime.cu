@@ -32,6 +32,7 @@ static bool g_side_rec[XMGD_SIDE_SLOTS];
 static buf g_chunk[XMGD_SIDE_SLOTS];
 
 cudaStream_t stream() { return g_stream; }
+int device() { return g_dev; }
 int num_sms() { return g_sms; }
 
 int
@@ -49,6 +50,8 @@ check(cudaError_t e, const char *what)
 } /* namespace xmg */
 
 using namespace xmg;
+
+extern "C" int xmgd_noalloc_setup(void);
 
 extern "C" int
 xmgd_init(void)
@@ -83,7 +86,9 @@ xmgd_init(void)
 	XMG_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold,
 	    &thr));
 	g_ready = 1;
-	return XMG_OK;
+	/* load the allocation-free dot's module now, so that its static
+	 * device array exists before the caller's first xmg_dot_noalloc */
+	return xmgd_noalloc_setup();
 }
 
 extern "C" int
@@ -293,6 +298,20 @@ xmg_timer_stop(void)
 }
 
 extern "C" long long xmg_kernel_launches(void) { return g_launches; }
+
+extern "C" int
+xmg_device_memory(size_t *free_bytes, size_t *total_bytes)
+{
+	int st;
+
+	if (free_bytes == NULL || total_bytes == NULL)
+		return xmg_seterr(XMG_EINVAL, "xmg_device_memory: NULL argument");
+	if ((st = xmgd_init()) != XMG_OK)
+		return st;
+	XMG_CK(cudaSetDevice(g_dev));
+	XMG_CK(cudaMemGetInfo(free_bytes, total_bytes));
+	return XMG_OK;
+}
 
 extern "C" void *
 xmg_host_alloc(size_t bytes)

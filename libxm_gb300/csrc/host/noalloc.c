@@ -27,6 +27,9 @@ xmg_dot_noalloc(const xm_tensor_t *a, const xm_tensor_t *b, const char *idxa,
 
 	if (result == NULL)
 		return xmg_seterr(XMG_EINVAL, "xmg_dot_noalloc: result is NULL");
+	if (a == NULL || b == NULL || idxa == NULL || idxb == NULL)
+		return xmg_seterr(XMG_EINVAL, "xmg_dot_noalloc: NULL tensor or "
+		    "index string");
 	if (a->allocator != b->allocator)
 		return xmg_seterr(XMG_EINVAL, "xmg_dot_noalloc: tensors must use "
 		    "same allocator");

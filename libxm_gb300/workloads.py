@@ -144,9 +144,11 @@ class Workload:
 
 
 def ladder(lib, alloc, o_sizes, v_sizes, seed=1, dtype=api.DOUBLE, z2=None,
-           with_c_fill=False):
+           with_c_fill=False, fill_data=True):
     """C(i,j,a,b) = sum_{c,d} A(i,j,c,d) B(c,d,a,b) with i<->j, c<->d, a<->b
-    antisymmetry (factor -1 derivative blocks) and optional Z2^3 labels."""
+    antisymmetry (factor -1 derivative blocks) and optional Z2^3 labels.
+    fill_data=False leaves the block data unwritten (for a copy of another
+    library's tensors of the same structure)."""
     bso = [o_sizes, o_sizes, v_sizes, v_sizes]
     bsv = [v_sizes] * 4
     sa, sb = make_space(lib, bso), make_space(lib, bsv)
@@ -159,9 +161,10 @@ def ladder(lib, alloc, o_sizes, v_sizes, seed=1, dtype=api.DOUBLE, z2=None,
     b = symmetric_tensor(lib, alloc, sb, dtype, LADDER_ANTISYM, alw_b)
     c = symmetric_tensor(lib, alloc, sa, dtype, LADDER_ANTISYM, alw_a)
     sa.free(); sb.free()
-    fill(a, seed * 3 + 1, LADDER_ANTISYM)
-    fill(b, seed * 3 + 2, LADDER_ANTISYM)
-    if with_c_fill:
+    if fill_data:
+        fill(a, seed * 3 + 1, LADDER_ANTISYM)
+        fill(b, seed * 3 + 2, LADDER_ANTISYM)
+    if with_c_fill and fill_data:
         fill(c, seed * 3 + 3, LADDER_ANTISYM)
     return Workload("ladder", a, b, c, ("ijcd", "cdab", "ijab"), 1.0, 0.0,
                     (LADDER_ANTISYM, LADDER_ANTISYM, LADDER_ANTISYM),
@@ -183,7 +186,7 @@ def cfg2_shape(seed=2):
     return o, v, lo, lv
 
 
-def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None):
+def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None, fill_data=True):
     """Uneven-block Z2^3-sparse FP64 ladder: o = 96 in 6 blocks of 8..24,
     v = 384 in 12 blocks of 16..48.  scale > 1 shrinks every block size by
     that factor (structure preserved) for quick parity runs; o_blocks /
@@ -197,7 +200,7 @@ def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None):
         o, lo = o[:o_blocks], lo[:o_blocks]
     if v_blocks:
         v, lv = v[:v_blocks], lv[:v_blocks]
-    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv))
+    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv), fill_data=fill_data)
     if o_blocks or v_blocks:
         w.name = "cfg2_subset_o%d_v%d" % (len(o), len(v))
     else:
@@ -231,7 +234,8 @@ def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None):
     return w
 
 
-def cfg3(lib, alloc, dtype=api.FLOAT, seed=3, o_blk=16, v_blk=32, no=4, nv=8):
+def cfg3(lib, alloc, dtype=api.FLOAT, seed=3, o_blk=16, v_blk=32, no=4, nv=8,
+         fill_data=True):
     """Ring term C(i,a,j,b) += sum_{k,c} A(k,i,c,a) B(j,k,b,c), beta = 1,
     C prefilled; (i,a) <-> (j,b) pair symmetry (+1) on C only, A and B
     fully canonical."""
@@ -242,12 +246,49 @@ def cfg3(lib, alloc, dtype=api.FLOAT, seed=3, o_blk=16, v_blk=32, no=4, nv=8):
     b = api.Tensor(lib, sab, dtype, alloc, canonical=True)
     c = symmetric_tensor(lib, alloc, sc, dtype, PAIR_SYM)
     sab.free(); sc.free()
-    fill(a, seed * 3 + 1)
-    fill(b, seed * 3 + 2)
-    fill(c, seed * 3 + 3, PAIR_SYM)
+    if fill_data:
+        fill(a, seed * 3 + 1)
+        fill(b, seed * 3 + 2)
+        fill(c, seed * 3 + 3, PAIR_SYM)
     return Workload("cfg3_ring_o64_v256", a, b, c, ("kica", "jkbc", "iajb"),
                     1.0, 1.0, (NO_SYM, NO_SYM, PAIR_SYM),
                     (seed * 3 + 1, seed * 3 + 2, seed * 3 + 3))
+
+
+def copy_data(src, dst):
+    """Write every canonical block of src into dst (same structure; the
+    values converted to dst's scalar type)."""
+    for blk in src.canonical_blocks():
+        dst.write_block(blk, src.read_block(blk).astype(dst.np))
+
+
+def sample_blocks(blocks, n, seed=0):
+    """A deterministic, seeded sample of n of the given blocks (all of
+    them when there are no more than n), in their original order."""
+    if len(blocks) <= n:
+        return list(blocks)
+    rng = np.random.default_rng(seed)
+    return [blocks[i] for i in sorted(rng.choice(len(blocks), n, replace=False))]
+
+
+def contract_sample(w, chosen, c0=None):
+    """Run w's contraction for the chosen canonical output blocks only:
+    the other canonical blocks of a fresh output structure are set to zero
+    blocks, so that a library that computes every canonical block does only
+    the chosen ones' work.  c0 gives the chosen blocks' initial values (for
+    beta != 0).  Returns {block: data} of the chosen blocks."""
+    c = w.c.structure()
+    keep = set(chosen)
+    for blk in w.c.canonical_blocks():
+        if blk not in keep:
+            c.lib.xm_tensor_set_zero_block(c.h, api.Dim.of(blk))
+    if c0 is not None:
+        for blk in chosen:
+            c.write_block(blk, c0[blk])
+    api.contract(w.alpha, w.a, w.b, w.beta, c, w.idxa, w.idxb, w.idxc)
+    out = {blk: c.read_block(blk) for blk in chosen}
+    c.free()
+    return out
 
 
 def read_canonical(t):

@@ -15,7 +15,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("XM_REFERENCE_SRC", "/root/reference/src")
+# the reference checkout's src/ directory: $XM_REFERENCE_SRC, else a
+# checkout named "reference" beside this repository
+REF_SRC = os.environ.get("XM_REFERENCE_SRC") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference", "src"))
 ORACLE_SO = os.path.join(HERE, "_build", "libxmoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libxmref.so")
 REF_FILES = ["alloc.c", "blockspace.c", "contract.c", "dim.c", "scalar.c",

@@ -82,3 +82,49 @@ def pair_structure_engine(lib, a, b, c, ia, ib, ic):
     lib.dll.xmg_contract_pairs.argtypes = [C.c_void_p] * 3 + [C.c_char_p] * 3 + [PAIR_CB]
     lib.check(lib.dll.xmg_contract_pairs(a.h, b.h, c.h, ia.encode(), ib.encode(), ic.encode(), f))
     return sorted(out, key=lambda x: (x[0], x[4], x[2], x[3], x[1].real, x[1].imag))
+
+
+def folded_cotangent(lib, al, dc):
+    """W = dC folded onto C's canonical blocks: every canonical block of dc
+    times its multiplicity (the sum of scalar^2 over the nonzero blocks
+    that share its data), on a tensor whose other blocks are zero."""
+    mult = {}
+    for blk in np.ndindex(*dc.nblocks()):
+        if dc.block_type(blk) != api.ZERO:
+            mult[dc.data_ptr(blk)] = mult.get(dc.data_ptr(blk), 0.0) + \
+                dc.block_scalar(blk).real ** 2
+    wt = api.Tensor(lib, None, dc.dtype, al,
+                    handle=lib.xm_tensor_create(lib.xm_tensor_get_block_space(dc.h),
+                                                dc.dtype, al.h))
+    for blk in dc.canonical_blocks():
+        wt.set_canonical(blk)
+        wt.write_block(blk, dc.read_block(blk) * mult[dc.data_ptr(blk)])
+    return wt
+
+
+def sampled_gradient(lib, al, t, wt, other, idx_w, idx_o, idx_t, alpha, sample, w_first):
+    """The oracle's gradient of L with respect to the sampled canonical
+    blocks of t: G = alpha * W * other at every nonzero position of t whose
+    data is a sampled block, folded back through each position's
+    permutation and scalar onto its canonical block."""
+    ptr2canon = {t.data_ptr(blk): blk for blk in t.canonical_blocks()}
+    keep = set(sample)
+    g = api.Tensor(lib, None, t.dtype, al,
+                   handle=lib.xm_tensor_create(lib.xm_tensor_get_block_space(t.h), t.dtype, al.h))
+    positions = []
+    for blk in np.ndindex(*t.nblocks()):
+        if t.block_type(blk) != api.ZERO and ptr2canon[t.data_ptr(blk)] in keep:
+            g.set_canonical(blk)
+            positions.append(blk)
+    if w_first:
+        api.contract(alpha, wt, other, 0.0, g, idx_w, idx_o, idx_t)
+    else:
+        api.contract(alpha, other, wt, 0.0, g, idx_o, idx_w, idx_t)
+    out = {blk: np.zeros(t.block_size(blk)) for blk in sample}
+    for blk in positions:
+        q = ptr2canon[t.data_ptr(blk)]
+        x = g.read_block(blk).reshape(t.block_dims(blk), order="F")
+        y = np.transpose(x, np.argsort(t.block_perm(blk)))
+        out[q] += t.block_scalar(blk).real * y.ravel(order="F")
+    g.free()
+    return out

@@ -29,14 +29,31 @@ def digest(x):
     return np.concatenate([[x.sum(), np.vdot(x, x).real], x[::97]])
 
 
-def test_dim_kat(oracle):
-    # test.c:1728-1764: offset round trip, index 0 fastest
-    for dims in ([5, 6, 3, 1], [1, 31, 16]):
-        for off, idx in enumerate(np.ndindex(*dims[::-1])):
-            pass
+@pytest.mark.parametrize("which", ["oracle", "engine"])
+def test_dim_kat(which, request):
+    # test.c:1728-1764: xm_dim_inc walks every index with index 0 fastest,
+    # xm_dim_offset numbers them sequentially and xm_dim_from_offset
+    # inverts it
+    lib = request.getfixturevalue(which)
+    P = api.C.POINTER(api.Dim)
+    lib.dll.xm_dim_offset.restype = api.C.c_size_t
+    lib.dll.xm_dim_offset.argtypes = [P, P]
+    lib.dll.xm_dim_from_offset.restype = api.Dim
+    lib.dll.xm_dim_from_offset.argtypes = [api.C.c_size_t, P]
+    lib.dll.xm_dim_inc.restype = None
+    lib.dll.xm_dim_inc.argtypes = [P, P]
+    for dims in ([5, 6, 3, 1], [1, 31, 16], [5, 2, 3, 2, 1, 2, 5, 4]):
+        d = api.Dim.of(dims)
+        idx = api.Dim.of([0] * len(dims))
+        for off, want in enumerate(np.ndindex(*dims[::-1])):
+            assert idx.tolist() == list(want[::-1])
+            assert lib.dll.xm_dim_offset(api.C.byref(idx), api.C.byref(d)) == off
+            back = lib.dll.xm_dim_from_offset(off, api.C.byref(d))
+            assert back.tolist() == idx.tolist()
+            lib.dll.xm_dim_inc(api.C.byref(idx), api.C.byref(d))
     d = api.Dim.of([5, 2, 3, 2, 1, 2, 5, 4])
-    oracle.xm_dim_dot.restype = api.C.c_size_t
-    assert oracle.xm_dim_dot(api.C.byref(d)) == 5 * 2 * 3 * 2 * 2 * 5 * 4
+    lib.xm_dim_dot.restype = api.C.c_size_t
+    assert lib.xm_dim_dot(api.C.byref(d)) == 5 * 2 * 3 * 2 * 2 * 5 * 4
 
 
 @pytest.mark.parametrize("which", ["oracle", "reference"])

@@ -61,7 +61,7 @@ def test_reference_arm_two_ranks_prints_once(tmp_path):
            "--nproc-per-node", "2", "--master-addr", "127.0.0.1",
            "--master-port", str(_free_port()), os.path.join(ROOT, "bench.py"),
            "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1",
-           "--scale", "4", "--cpu-seconds", "1"]
+           "--scale", "4"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -72,3 +72,5 @@ def test_reference_arm_two_ranks_prints_once(tmp_path):
         assert d["unit"] == "TFLOP/s" and d["value"] > 0
         assert d["e2e"]["h2d_bytes_per_step"] == 0
         assert d["cpu_baseline"]["cores"] >= 1
+        # one step is the whole contraction
+        assert d["cpu_baseline"]["sample"].startswith("262 of 262 ")
