@@ -203,6 +203,36 @@ long long xmg_kernel_launches(void);
 void *xmg_host_alloc(size_t bytes);
 void xmg_host_free(void *p);
 
+/* An allocator whose blocks live in page-locked host memory, the
+ * counterpart of the reference's RAM allocator (xm_allocator_create(NULL)
+ * in the reference, alloc.c:233-239; here that call gives GPU memory).
+ * Handles are host addresses; xm_allocator_read/write and the block
+ * read/write calls are plain memory copies.  xm_contract streams the
+ * operands of such tensors through HBM on every call: a's blocks (and c's
+ * when beta != 0) and b's first batch are copied in, then each further
+ * batch of b (about 1/XMG_HOST_BATCHES of it, default 4, at most the
+ * staging region) is copied on a side stream while the previous batch is
+ * contracted, and c is copied back before the call returns.  The
+ * streamed plan of the last such contraction (batches, HBM regions, the
+ * device plans and their graphs) is kept while the tensors' block
+ * structures and the call's arguments stay the same (XMG_STREAM_CACHE=0
+ * disables that; xmg_plan_cache_clear releases it).  Element-wise
+ * operations stage the blocks they touch.  NULL if the engine cannot
+ * start. */
+xm_allocator_t *xmg_allocator_create_host(void);
+
+/* Write (read) n blocks in one call: blks[i] from (into) the host buffer
+ * bufs[i], of xm_tensor_get_block_bytes bytes each.  For tensors in GPU
+ * memory the copies are queued back to back (one cudaMemcpyAsync per
+ * block) and waited for once; buffers may be reused on return, as after
+ * xm_tensor_write_block.  Same rules as the one-block calls (canonical
+ * blocks only for writes, no zero blocks for reads), reported as
+ * XMG_EINVAL before any data moves.  Returns XMG_* status. */
+int xmg_tensor_write_blocks(xm_tensor_t *t, size_t n, const xm_dim_t *blks,
+    const void *const *bufs);
+int xmg_tensor_read_blocks(const xm_tensor_t *t, size_t n,
+    const xm_dim_t *blks, void *const *bufs);
+
 /* The engine runs on device ordinal $XMG_DEVICE (default 0), chosen at
  * the first call that needs the GPU. */
 

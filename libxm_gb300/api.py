@@ -141,6 +141,9 @@ _GB_SIGS = {
     "xmg_host_alloc": (_P, [C.c_size_t]),
     "xmg_host_free": (None, [_P]),
     "xmg_device_memory": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "xmg_allocator_create_host": (_P, []),
+    "xmg_tensor_write_blocks": (C.c_int, [_P, C.c_size_t, C.POINTER(Dim), C.POINTER(_P)]),
+    "xmg_tensor_read_blocks": (C.c_int, [_P, C.c_size_t, C.POINTER(Dim), C.POINTER(_P)]),
 }
 
 
@@ -201,11 +204,16 @@ class BlockSpace:
 
 
 class Allocator:
-    def __init__(self, lib, path=None):
+    def __init__(self, lib, path=None, host=False):
+        """GPU memory (path None), a pagefile (path), or, on the engine,
+        page-locked host memory (host=True: xmg_allocator_create_host)."""
         self.lib = lib
-        self.h = lib.xm_allocator_create(path.encode() if path else None)
+        if host:
+            self.h = lib.xmg_allocator_create_host()
+        else:
+            self.h = lib.xm_allocator_create(path.encode() if path else None)
         if not self.h:
-            raise XmError("xm_allocator_create failed")
+            raise XmError("allocator creation failed")
 
     def destroy(self):
         if self.h:
@@ -283,6 +291,20 @@ class Tensor:
         a = np.empty(n, dtype=self.np)
         self.lib.xm_tensor_read_block(self.h, Dim.of(blk), a.ctypes.data)
         return a
+
+    def write_blocks(self, blocks, ptrs):
+        """xmg_tensor_write_blocks: blocks[i] from the host address ptrs[i]."""
+        n = len(blocks)
+        dims = (Dim * max(1, n))(*[Dim.of(b) for b in blocks])
+        bufs = (C.c_void_p * max(1, n))(*ptrs)
+        self.lib.check(self.lib.xmg_tensor_write_blocks(self.h, n, dims, bufs))
+
+    def read_blocks(self, blocks, ptrs):
+        """xmg_tensor_read_blocks: blocks[i] into the host address ptrs[i]."""
+        n = len(blocks)
+        dims = (Dim * max(1, n))(*[Dim.of(b) for b in blocks])
+        bufs = (C.c_void_p * max(1, n))(*ptrs)
+        self.lib.check(self.lib.xmg_tensor_read_blocks(self.h, n, dims, bufs))
 
     def get_element(self, idx):
         return self.lib.xm_tensor_get_element(self.h, Dim.of(idx)).value()

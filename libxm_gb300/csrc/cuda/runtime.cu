@@ -130,6 +130,22 @@ xmgd_d2h(void *dst, uint64_t src, size_t bytes)
 }
 
 extern "C" int
+xmgd_h2d_async(uint64_t dst, const void *src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst, src, bytes,
+	    cudaMemcpyHostToDevice, g_stream));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_d2h_async(void *dst, uint64_t src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync(dst, (const void *)(uintptr_t)src, bytes,
+	    cudaMemcpyDeviceToHost, g_stream));
+	return XMG_OK;
+}
+
+extern "C" int
 xmgd_d2d(uint64_t dst, uint64_t src, size_t bytes)
 {
 	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst,
@@ -262,6 +278,22 @@ xmgd_side_fetch(int slot, uint64_t src, size_t bytes)
 }
 
 extern "C" int
+xmgd_side_put(uint64_t dst, const void *src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync((void *)(uintptr_t)dst, src, bytes,
+	    cudaMemcpyHostToDevice, g_side));
+	return XMG_OK;
+}
+
+extern "C" int
+xmgd_side_get(void *dst, uint64_t src, size_t bytes)
+{
+	XMG_CK(cudaMemcpyAsync(dst, (const void *)(uintptr_t)src, bytes,
+	    cudaMemcpyDeviceToHost, g_side));
+	return XMG_OK;
+}
+
+extern "C" int
 xmgd_side_sync(void)
 {
 	XMG_CK(cudaStreamSynchronize(g_side));
@@ -311,6 +343,21 @@ xmg_device_memory(size_t *free_bytes, size_t *total_bytes)
 	XMG_CK(cudaSetDevice(g_dev));
 	XMG_CK(cudaMemGetInfo(free_bytes, total_bytes));
 	return XMG_OK;
+}
+
+extern "C" int
+xmgd_host_alloc(size_t bytes, void **hptr)
+{
+	XMG_CK(cudaSetDevice(g_dev));
+	XMG_CK(cudaHostAlloc(hptr, bytes, cudaHostAllocDefault));
+	return XMG_OK;
+}
+
+extern "C" void
+xmgd_host_free(void *p)
+{
+	if (p)
+		cudaFreeHost(p);
 }
 
 extern "C" void *

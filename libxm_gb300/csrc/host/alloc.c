@@ -12,6 +12,12 @@
  * offset | page count << 32, I/O in chunks of at most 1 GiB -- the
  * reference's pagefile scheme (alloc.c:40-145, 249-300).  The contraction
  * engine stages the pagefile blocks it touches into HBM (device views).
+ *
+ * xmg_allocator_create_host(): every allocation is page-locked host memory
+ * (the reference's RAM allocator, alloc.c:233-239, kept in host memory)
+ * and the handle is its host address.  read/write are memcpy; operations
+ * stage the blocks they touch into HBM like pagefile blocks, but copy them
+ * straight from the block's own pinned memory.
  */
 #include <errno.h>
 #include <fcntl.h>
@@ -26,6 +32,7 @@
 
 struct xm_allocator {
 	char *path;
+	int host;                 /* blocks in page-locked host memory */
 	int fd;
 	uint64_t file_bytes;
 	unsigned char *used;      /* one bit per page */
@@ -42,7 +49,34 @@ static void bit_clr(unsigned char *b, uint64_t i) { b[i >> 3] &= (unsigned char)
 int
 xmg_alloc_is_device(const xm_allocator_t *a)
 {
-	return a->path == NULL;
+	return a->path == NULL && !a->host;
+}
+
+int
+xmg_alloc_is_host(const xm_allocator_t *a)
+{
+	return a->host;
+}
+
+xm_allocator_t *
+xmg_allocator_create_host(void)
+{
+	xm_allocator_t *a;
+
+	if (xmgd_init() != XMG_OK) {
+		fprintf(stderr, "libxm: %s\n", xmg_last_error());
+		return NULL;
+	}
+	if ((a = calloc(1, sizeof *a)) == NULL) {
+		perror("calloc");
+		return NULL;
+	}
+	xmg_hmap_init(&a->live);
+	xmg_hmap_init(&a->views);
+	xmg_hmap_init(&a->bviews);
+	a->fd = -1;
+	a->host = 1;
+	return a;
 }
 
 xm_allocator_t *
@@ -149,6 +183,19 @@ xm_allocator_allocate(xm_allocator_t *a, size_t bytes)
 
 	if (bytes == 0)
 		return XM_NULL_PTR;
+	if (a->host) {
+		void *p;
+		if (xmgd_host_alloc(bytes, &p) != XMG_OK) {
+			fprintf(stderr, "libxm: %s\n", xmg_last_error());
+			return XM_NULL_PTR;
+		}
+		h = (uint64_t)(uintptr_t)p;
+		if (xmg_hmap_put(&a->live, h, bytes)) {
+			xmgd_host_free(p);
+			return XM_NULL_PTR;
+		}
+		return h;
+	}
 	if (a->path == NULL) {
 		if (xmgd_alloc(bytes, &h) != XMG_OK) {
 			fprintf(stderr, "libxm: %s\n", xmg_last_error());
@@ -192,12 +239,33 @@ file_io(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes, int wr)
 	return XMG_OK;
 }
 
+/* xm_allocator_read (wr = 0) / write (wr = 1) with a status instead of
+ * an exit */
+int
+xmg_alloc_io(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes, int wr)
+{
+	if (h == XM_NULL_PTR)
+		return xmg_seterr(XMG_EINVAL, "data pointer is NULL");
+	if (a->host) {
+		if (wr)
+			memcpy((void *)(uintptr_t)h, mem, bytes);
+		else
+			memcpy(mem, (const void *)(uintptr_t)h, bytes);
+		return XMG_OK;
+	}
+	if (a->path == NULL)
+		return wr ? xmgd_h2d(h, mem, bytes) : xmgd_d2h(mem, h, bytes);
+	return file_io(a, h, mem, bytes, wr);
+}
+
 void
 xm_allocator_read(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes)
 {
 	if (h == XM_NULL_PTR)
 		xm_fatal("%s: data pointer is NULL", __func__);
-	if (a->path == NULL)
+	if (a->host)
+		memcpy(mem, (const void *)(uintptr_t)h, bytes);
+	else if (a->path == NULL)
 		xmg_die_on(xmgd_d2h(mem, h, bytes));
 	else
 		xmg_die_on(file_io(a, h, mem, bytes, 0));
@@ -208,7 +276,9 @@ xm_allocator_write(xm_allocator_t *a, uint64_t h, const void *mem, size_t bytes)
 {
 	if (h == XM_NULL_PTR)
 		xm_fatal("%s: data pointer is NULL", __func__);
-	if (a->path == NULL)
+	if (a->host)
+		memcpy((void *)(uintptr_t)h, mem, bytes);
+	else if (a->path == NULL)
 		xmg_die_on(xmgd_h2d(h, mem, bytes));
 	else
 		xmg_die_on(file_io(a, h, (void *)mem, bytes, 1));
@@ -221,6 +291,11 @@ xm_allocator_deallocate(xm_allocator_t *a, uint64_t h)
 
 	if (h == XM_NULL_PTR)
 		return;
+	if (a->host) {
+		xmg_hmap_del(&a->live, h);
+		xmgd_host_free((void *)(uintptr_t)h);
+		return;
+	}
 	if (a->path == NULL) {
 		xmg_hmap_del(&a->live, h);
 		xmg_die_on(xmgd_free(h));
@@ -240,7 +315,7 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 	void *pin;
 	int st;
 
-	if (a->path == NULL) {
+	if (xmg_alloc_is_device(a)) {
 		*dptr = h;
 		return XMG_OK;
 	}
@@ -249,9 +324,12 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 		return XMG_OK;
 	if ((st = xmgd_alloc(bytes, &d)) != XMG_OK)
 		return st;
-	if ((st = xmgd_pinned(bytes, &pin)) != XMG_OK ||
-	    (st = file_io(a, h, pin, bytes, 0)) != XMG_OK ||
-	    (st = xmgd_h2d(d, pin, bytes)) != XMG_OK) {
+	if (a->host)
+		st = xmgd_h2d(d, (const void *)(uintptr_t)h, bytes);
+	else if ((st = xmgd_pinned(bytes, &pin)) == XMG_OK &&
+	    (st = file_io(a, h, pin, bytes, 0)) == XMG_OK)
+		st = xmgd_h2d(d, pin, bytes);
+	if (st != XMG_OK) {
 		xmgd_free(d);
 		return st;
 	}
@@ -263,7 +341,7 @@ xmg_alloc_device_view(xm_allocator_t *a, uint64_t h, size_t bytes,
 	return XMG_OK;
 }
 
-/* Write a staged view back to the pagefile. */
+/* Write a staged view back to the pagefile (or the host block). */
 int
 xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes)
 {
@@ -271,10 +349,12 @@ xmg_alloc_commit_view(xm_allocator_t *a, uint64_t h, size_t bytes)
 	void *pin;
 	int st;
 
-	if (a->path == NULL)
+	if (xmg_alloc_is_device(a))
 		return XMG_OK;
 	if (!xmg_hmap_get(&a->views, h, &d) && !xmg_hmap_get(&a->bviews, h, &d))
 		return xmg_seterr(XMG_EINVAL, "no staged view for handle");
+	if (a->host)
+		return xmgd_d2h((void *)(uintptr_t)h, d, bytes);
 	if ((st = xmgd_pinned(bytes, &pin)) != XMG_OK ||
 	    (st = xmgd_d2h(pin, d, bytes)) != XMG_OK)
 		return st;
@@ -287,7 +367,7 @@ xmg_alloc_release_views(xm_allocator_t *a, int write_back)
 	size_t i;
 
 	(void)write_back;
-	if (a->path == NULL)
+	if (xmg_alloc_is_device(a))
 		return XMG_OK;
 	for (i = 0; i < a->views.cap; i++)
 		if (a->views.keys[i] != XMG_HMAP_EMPTY)
@@ -311,10 +391,10 @@ xmg_alloc_bulk_views(xm_allocator_t *a, uint64_t bulk, const uint64_t *h,
 {
 	size_t i;
 
-	if (a->path == NULL || a->bulk) {
+	if (xmg_alloc_is_device(a) || a->bulk) {
 		xmgd_free(bulk);
-		return xmg_seterr(XMG_EINVAL, "bulk views: pagefile allocator "
-		    "without bulk views expected");
+		return xmg_seterr(XMG_EINVAL, "bulk views: pagefile or host "
+		    "allocator without bulk views expected");
 	}
 	a->bulk = bulk;
 	for (i = 0; i < n; i++)
@@ -347,6 +427,11 @@ xm_allocator_destroy(xm_allocator_t *a)
 			perror("close");
 		if (unlink(a->path))
 			perror("unlink");
+	} else if (a->host) {
+		xmg_alloc_release_views(a, 0);
+		for (i = 0; i < a->live.cap; i++)
+			if (a->live.keys[i] != XMG_HMAP_EMPTY)
+				xmgd_host_free((void *)(uintptr_t)a->live.keys[i]);
 	} else {
 		/* blocks still allocated when the allocator goes away */
 		for (i = 0; i < a->live.cap; i++)
@@ -369,6 +454,10 @@ xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
 {
 	ssize_t r;
 
+	if (a->host) {
+		memcpy(mem, (const char *)(uintptr_t)h + byte_off, bytes);
+		return XMG_OK;
+	}
 	if (a->path == NULL)
 		return xmgd_d2h(mem, h + byte_off, bytes);
 	r = pread(a->fd, mem, bytes, page_offset(h) + (off_t)byte_off);
@@ -382,6 +471,10 @@ xmg_alloc_write_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
 {
 	ssize_t r;
 
+	if (a->host) {
+		memcpy((char *)(uintptr_t)h + byte_off, mem, bytes);
+		return XMG_OK;
+	}
 	if (a->path == NULL)
 		return xmg_seterr(XMG_EINVAL, "write_range: pagefile allocator "
 		    "expected");

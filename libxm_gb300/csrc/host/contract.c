@@ -825,6 +825,25 @@ stage_threads(void)
 	return n < 1 ? 1 : n > XMGD_SIDE_SLOTS / 2 ? XMGD_SIDE_SLOTS / 2 : n;
 }
 
+/* host-allocator blocks: one cudaMemcpyAsync per block straight from (or
+ * into) the block's own page-locked memory, queued on the side stream */
+static void
+io_host(struct io_job *j)
+{
+	size_t i;
+	int st = xmgd_bind_thread();
+
+	for (i = 0; st == XMG_OK && i < j->n; i++)
+		st = j->wr ? xmgd_side_get((void *)(uintptr_t)j->h[i], j->dst[i],
+		    j->sz[i]) : xmgd_side_put(j->dst[i],
+		    (const void *)(uintptr_t)j->h[i], j->sz[i]);
+	if (xmgd_side_sync() != XMG_OK && st == XMG_OK)
+		st = XMG_ECUDA;
+	if (st != XMG_OK)
+		snprintf(j->err, sizeof j->err, "%s", xmg_last_error());
+	j->status = st;
+}
+
 static void *
 io_main(void *arg)
 {
@@ -832,6 +851,11 @@ io_main(void *arg)
 	struct io_worker r[XMGD_SIDE_SLOTS / 2];
 	pthread_t th[XMGD_SIDE_SLOTS / 2];
 	int nw = stage_threads(), w, started = 0, st = XMG_OK;
+
+	if (xmg_alloc_is_host(j->al)) {
+		io_host(j);
+		return NULL;
+	}
 
 	for (w = 0; w < nw; w++) {
 		r[w].j = j;
@@ -968,23 +992,27 @@ commit_c(xm_tensor_t *c, int st)
 }
 
 /*
- * Views of a's and c's canonical blocks (one pagefile allocator) in one
- * HBM buffer, registered with the allocator; returns the blocks to read
- * into them (c's only when read_c: for beta = 0 the contraction
- * overwrites c, as the reference zeroes it, contract.c:155-158).
+ * Views of a's and c's canonical blocks (one pagefile or host allocator)
+ * in one HBM buffer *bulk, each block at a 256-byte aligned offset: vmap
+ * maps every block's handle to its address.  Returns the blocks to read
+ * into it (c's only when read_c: for beta = 0 the contraction overwrites
+ * c, as the reference zeroes it, contract.c:155-158) and c's canonical
+ * blocks, the ones to write back.
  */
 static int
 bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
-    uint64_t **rh, uint64_t **rsz, uint64_t **rd, size_t *nr)
+    uint64_t *bulk, xmg_hmap_t *vmap, uint64_t **rh, uint64_t **rsz,
+    uint64_t **rd, size_t *nr, uint64_t **ch, uint64_t **csz, uint64_t **cd,
+    size_t *ncw)
 {
 	const xm_tensor_t *t[2] = {a, c};
 	xm_dim_t *list[2] = {NULL, NULL};
 	size_t n[2] = {0, 0}, cnt = 0, m = 0, q, s;
-	uint64_t *h, *sz, *d, off = 0, bulk = 0;
+	uint64_t *h, *sz, *d, off = 0, v;
 	char *rdf;
-	xmg_hmap_t seen;
 	int st = XMG_OK;
 
+	*bulk = 0;
 	for (s = 0; s < 2; s++) {
 		xm_tensor_get_canonical_block_list(t[s], &list[s], &n[s]);
 		cnt += n[s];
@@ -993,17 +1021,19 @@ bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
 	sz = malloc((cnt + 1) * sizeof *sz);
 	d = malloc((cnt + 1) * sizeof *d);
 	rdf = malloc(cnt + 1);
-	if (!h || !sz || !d || !rdf)
+	*ch = malloc((n[1] + 1) * sizeof **ch);
+	*csz = malloc((n[1] + 1) * sizeof **csz);
+	*cd = malloc((n[1] + 1) * sizeof **cd);
+	if (!h || !sz || !d || !rdf || !*ch || !*csz || !*cd)
 		xm_fatal("%s: out of memory", __func__);
-	xmg_hmap_init(&seen);
 	for (s = 0; s < 2; s++)
 		for (q = 0; q < n[s]; q++) {
-			uint64_t hq = xm_tensor_get_block_data_ptr(t[s], list[s][q]), v;
-			if (xmg_hmap_get(&seen, hq, &v)) {
+			uint64_t hq = xm_tensor_get_block_data_ptr(t[s], list[s][q]);
+			if (xmg_hmap_get(vmap, hq, &v)) {
 				rdf[v] |= s == 0 || read_c;
 				continue;
 			}
-			if (xmg_hmap_put(&seen, hq, m))
+			if (xmg_hmap_put(vmap, hq, m))
 				xm_fatal("%s: out of memory", __func__);
 			h[m] = hq;
 			sz[m] = xm_tensor_get_block_bytes(t[s], list[s][q]);
@@ -1012,14 +1042,23 @@ bulk_views(const xm_tensor_t *a, const xm_tensor_t *c, int read_c,
 			off += (sz[m] + STAGE_ALIGN - 1) / STAGE_ALIGN * STAGE_ALIGN;
 			m++;
 		}
-	xmg_hmap_free(&seen);
+	if (m > 0 && (st = xmgd_alloc(off, bulk)) == XMG_OK)
+		for (q = 0; q < m; q++) {
+			d[q] += *bulk;
+			/* the map now gives addresses */
+			if (xmg_hmap_put(vmap, h[q], d[q]))
+				xm_fatal("%s: out of memory", __func__);
+		}
+	*ncw = 0;
+	for (q = 0; st == XMG_OK && q < n[1]; q++) {
+		uint64_t hq = xm_tensor_get_block_data_ptr(c, list[1][q]);
+		(*ch)[*ncw] = hq;
+		(*csz)[*ncw] = xm_tensor_get_block_bytes(c, list[1][q]);
+		xmg_hmap_get(vmap, hq, &(*cd)[*ncw]);
+		(*ncw)++;
+	}
 	free(list[0]);
 	free(list[1]);
-	if (m > 0 && (st = xmgd_alloc(off, &bulk)) == XMG_OK) {
-		for (q = 0; q < m; q++)
-			d[q] += bulk;
-		st = xmg_alloc_bulk_views(a->allocator, bulk, h, d, m);
-	}
 	/* keep the blocks to read, in order */
 	*nr = 0;
 	for (q = 0; st == XMG_OK && q < m; q++)
@@ -1071,12 +1110,16 @@ batch_buf_free(struct batch_buf *bb)
 	memset(bb, 0, sizeof *bb);
 }
 
-/* a data handle's device address: its staged view, or the handle itself
- * when there is no allocator (host-side checks) */
+/* a data handle's device address: its staged view in vmap, or the
+ * handle itself when there is no map (host-side checks) */
 static uint64_t
-handle_addr(const xm_allocator_t *al, uint64_t h)
+handle_addr(const xmg_hmap_t *vmap, uint64_t h)
 {
-	return al ? xmg_alloc_view_addr(al, h) : h;
+	uint64_t d;
+
+	if (vmap == NULL)
+		return h;
+	return xmg_hmap_get(vmap, h, &d) ? d : 0;
 }
 
 /* the distinct b blocks of a collected plan, in handle (file) order */
@@ -1135,7 +1178,7 @@ form_batches(const struct hsz *u, size_t nu, size_t region, uint64_t *off,
 }
 
 static int
-batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xm_allocator_t *al,
+batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xmg_hmap_t *al,
     struct batch_buf *bb, xm_scalar_t alpha, xm_scalar_t beta, int prec,
     xmgd_contract_t *dp)
 {
@@ -1358,133 +1401,284 @@ done:
 }
 
 /*
- * Pagefile path.  Returns 0 when the contraction should run through the
- * in-core path (b in GPU memory or b aliasing a or c), else 1 with the
- * status in *st.  b is streamed in batches when its blocks exceed the
- * staging budget, else staged whole as a single batch.
+ * A streamed contraction, kept across calls: the whole plan's batches of
+ * b (data handles, bytes, device addresses in the two regions), the
+ * regions themselves, the HBM buffer holding a's and c's blocks, and one
+ * device plan per batch.  A call whose tensors, structure generations,
+ * index strings, scalars, precision and staging sizes match the kept one
+ * reuses all of it: no planning, no device allocation, the batch plans'
+ * captured graphs replayed.  Only the data moves.
+ */
+struct stream_plan {
+	const xm_tensor_t *a, *b, *c;
+	uint64_t ga, gb, gc;
+	char idx[3][16];
+	xm_scalar_t alpha, beta;
+	int precision, keep;
+	size_t budget, region;
+	/* b's distinct blocks in file order, batch k = bstart[k] ..
+	 * bstart[k + 1] - 1 */
+	size_t nu, nb, *bstart;
+	uint64_t *H, *SZ, *D, total, rbytes, reg[2];
+	/* a's and c's blocks in one buffer: the ones read before batch 0
+	 * (R*) and c's canonical blocks, written back after the last (C*) */
+	uint64_t bulk;
+	size_t nr, ncw;
+	uint64_t *RH, *RSZ, *RD, *CH, *CSZ, *CD;
+	xmg_hmap_t vmap;            /* a's and c's handles -> addresses */
+	xmgd_plan_t **bp;           /* per batch, built on first use */
+	double *bflops;
+	int *bnpairs;
+	double flops;
+	int ncb;
+};
+
+static struct stream_plan *g_sp;    /* the kept streamed contraction */
+
+static void
+sp_free(struct stream_plan *sp)
+{
+	size_t k;
+
+	if (sp == NULL)
+		return;
+	if (sp->bp)
+		for (k = 0; k < sp->nb; k++)
+			if (sp->bp[k])
+				xmgd_plan_free(sp->bp[k]);
+	xmgd_sync();
+	if (sp->reg[0])
+		xmgd_free(sp->reg[0]);
+	if (sp->reg[1])
+		xmgd_free(sp->reg[1]);
+	if (sp->bulk)
+		xmgd_free(sp->bulk);
+	xmg_hmap_free(&sp->vmap);
+	free(sp->bstart); free(sp->H); free(sp->SZ); free(sp->D);
+	free(sp->RH); free(sp->RSZ); free(sp->RD);
+	free(sp->CH); free(sp->CSZ); free(sp->CD);
+	free(sp->bp); free(sp->bflops); free(sp->bnpairs);
+	free(sp);
+}
+
+static int
+sp_match(const struct stream_plan *sp, xm_scalar_t alpha,
+    const xm_tensor_t *a, const xm_tensor_t *b, xm_scalar_t beta,
+    const xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, int prec, size_t budget, size_t region)
+{
+	return sp != NULL && sp->a == a && sp->b == b && sp->c == c &&
+	    sp->ga == a->gen && sp->gb == b->gen && sp->gc == c->gen &&
+	    sp->alpha == alpha && sp->beta == beta && sp->precision == prec &&
+	    sp->budget == budget && sp->region == region &&
+	    strcmp(sp->idx[0], idxa) == 0 && strcmp(sp->idx[1], idxb) == 0 &&
+	    strcmp(sp->idx[2], idxc) == 0;
+}
+
+/* host-allocator b: batches of about total / XMG_HOST_BATCHES bytes (at
+ * most `region`), so that the copies of one batch overlap the kernels of
+ * the previous one */
+static size_t
+host_region(uint64_t total, size_t nu, size_t region)
+{
+	const char *e = getenv("XMG_HOST_BATCHES");
+	uint64_t nb = e ? (uint64_t)atoi(e) : 4, r;
+
+	if (nb < 1)
+		nb = 1;
+	r = (total + nb - 1) / nb + (uint64_t)STAGE_ALIGN * (nu / nb + 2);
+	return r < region ? (size_t)r : region;
+}
+
+/*
+ * The batches, regions and staged views of a streamed contraction (no
+ * device plans yet).  Returns XMG_OK with *sp set, or a status; *incore
+ * is set when the in-core path should run instead (no GEMMs, or a
+ * structure error the in-core path reports).
  */
 static int
-contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
-    const xm_tensor_t *b, xm_scalar_t beta, xm_tensor_t *c,
-    const char *idxa, const char *idxb, const char *idxc, int prec, int *st)
+sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
+    xm_scalar_t beta, xm_tensor_t *c, const char *idxa, const char *idxb,
+    const char *idxc, int prec, size_t budget, size_t region, plan_t *p0,
+    struct stream_plan **out, int *incore)
 {
-	plan_t p0;
-	struct batch_buf bb = {NULL, NULL, NULL, NULL, NULL, NULL};
+	struct stream_plan *sp;
 	struct hsz *u = NULL;
-	uint64_t *H = NULL, *SZ = NULL, *OFF = NULL, *D = NULL, total = 0;
-	uint64_t *VH = NULL, *VSZ = NULL, *VD = NULL, *JH = NULL, *JSZ = NULL,
-	    *JD = NULL;
-	size_t nv = 0;
-	uint64_t reg[2] = {0, 0}, rbytes = 0;
-	size_t budget, region, nu = 0, i, *bstart = NULL, nb = 0, k;
-	struct io_job io[2];
-	xmg_hmap_t filt;
-	xmg_stats_t acc;
-	double tw;
-	int used_all = XMG_PREC_EMU64;
+	uint64_t *OFF = NULL;
+	size_t i, k;
+	int st;
 
-	if (xmg_alloc_is_device(b->allocator) || b == a || b == c)
-		return 0;
-	if (!g_stage_budget)
-		g_stage_budget = env_bytes("XMG_STAGE_BUDGET_GB", 180);
-	if (!g_stage_region)
-		g_stage_region = env_bytes("XMG_STAGE_REGION_GB", 32);
-	budget = g_stage_budget;
-	region = g_stage_region;
-	/* the whole plan once, with data handles for addresses; every
-	 * batch's plan is cut from it */
-	double tp = now_ms();
-	init_plan(&p0);
-	p0.collect = 1;
-	if (check_contract(a, b, c, idxa, idxb, idxc, &p0) != XMG_OK ||
-	    build_plan(alpha, a, b, c, &p0, 2) != XMG_OK) {
-		plan_free(&p0);
-		return 0;	/* the in-core path reports it */
+	*out = NULL;
+	*incore = 0;
+	p0->collect = 1;
+	if (check_contract(a, b, c, idxa, idxb, idxc, p0) != XMG_OK ||
+	    build_plan(alpha, a, b, c, p0, 2) != XMG_OK) {
+		*incore = 1;	/* the in-core path reports it */
+		return XMG_OK;
 	}
-	tp = now_ms() - tp;
+	if ((sp = calloc(1, sizeof *sp)) == NULL)
+		xm_fatal("%s: out of memory", __func__);
+	xmg_hmap_init(&sp->vmap);
+	sp->a = a; sp->b = b; sp->c = c;
+	sp->ga = a->gen; sp->gb = b->gen; sp->gc = c->gen;
+	sp->alpha = alpha; sp->beta = beta; sp->precision = prec;
+	sp->budget = budget; sp->region = region;
+	sp->keep = strlen(idxa) < 16 && strlen(idxb) < 16 && strlen(idxc) < 16;
+	if (sp->keep) {
+		strcpy(sp->idx[0], idxa);
+		strcpy(sp->idx[1], idxb);
+		strcpy(sp->idx[2], idxc);
+	}
+	sp->flops = p0->flops;
+	sp->ncb = p0->ncb;
 	/* distinct b blocks in file order */
-	nu = distinct_b(&p0, &u);
-	if (nu == 0) {
+	sp->nu = distinct_b(p0, &u);
+	if (sp->nu == 0) {
 		/* no GEMMs (alpha = 0 or no nonzero pair): the in-core path
 		 * applies beta to c */
 		free(u);
-		plan_free(&p0);
-		return 0;
+		sp_free(sp);
+		*incore = 1;
+		return XMG_OK;
 	}
-	for (i = 0; i < nu; i++)
-		total += u[i].sz;
-	/* within the budget b is staged whole: one batch, still read by the
-	 * parallel readers */
-	if (total <= budget)
-		region = total + nu * STAGE_ALIGN;
-	/* batches of at most `region` bytes (256-byte aligned offsets) */
-	H = malloc(nu * sizeof *H);
-	SZ = malloc(nu * sizeof *SZ);
-	OFF = malloc(nu * sizeof *OFF);
-	D = malloc(nu * sizeof *D);
-	bstart = malloc((nu + 1) * sizeof *bstart);
-	if (!H || !SZ || !OFF || !D || !bstart)
+	for (i = 0; i < sp->nu; i++)
+		sp->total += u[i].sz;
+	/* within the budget a pagefile b is staged whole: one batch, still
+	 * read by the parallel readers; a host b is always streamed */
+	if (xmg_alloc_is_host(b->allocator))
+		region = host_region(sp->total, sp->nu, region);
+	else if (sp->total <= budget)
+		region = sp->total + sp->nu * STAGE_ALIGN;
+	sp->H = malloc(sp->nu * sizeof *sp->H);
+	sp->SZ = malloc(sp->nu * sizeof *sp->SZ);
+	sp->D = malloc(sp->nu * sizeof *sp->D);
+	OFF = malloc(sp->nu * sizeof *OFF);
+	sp->bstart = malloc((sp->nu + 1) * sizeof *sp->bstart);
+	if (!sp->H || !sp->SZ || !sp->D || !OFF || !sp->bstart)
 		xm_fatal("%s: out of memory", __func__);
-	for (i = 0; i < nu; i++) {
-		H[i] = u[i].h;
-		SZ[i] = u[i].sz;
+	for (i = 0; i < sp->nu; i++) {
+		sp->H[i] = u[i].h;
+		sp->SZ[i] = u[i].sz;
 	}
-	if ((*st = form_batches(u, nu, region, OFF, bstart, &nb, &rbytes)) !=
-	    XMG_OK)
-		goto out;
+	st = form_batches(u, sp->nu, region, OFF, sp->bstart, &sp->nb,
+	    &sp->rbytes);
+	free(u);
+	if (st == XMG_OK) {
+		sp->bp = calloc(sp->nb, sizeof *sp->bp);
+		sp->bflops = calloc(sp->nb, sizeof *sp->bflops);
+		sp->bnpairs = calloc(sp->nb, sizeof *sp->bnpairs);
+		if (!sp->bp || !sp->bflops || !sp->bnpairs)
+			xm_fatal("%s: out of memory", __func__);
+	}
+	if (st == XMG_OK)
+		st = xmgd_alloc(sp->rbytes, &sp->reg[0]);
+	if (st == XMG_OK && sp->nb > 1)
+		st = xmgd_alloc(sp->rbytes, &sp->reg[1]);
+	/* every b block's address in its batch's region */
+	for (k = 0; st == XMG_OK && k < sp->nb; k++)
+		for (i = sp->bstart[k]; i < sp->bstart[k + 1]; i++)
+			sp->D[i] = sp->reg[k & 1] + OFF[i];
+	free(OFF);
+	/* a's and c's blocks as views in one buffer */
+	if (st == XMG_OK)
+		st = bulk_views(a, c, creal(beta) != 0 || cimag(beta) != 0,
+		    &sp->bulk, &sp->vmap, &sp->RH, &sp->RSZ, &sp->RD, &sp->nr,
+		    &sp->CH, &sp->CSZ, &sp->CD, &sp->ncw);
+	if (st == XMG_OK)
+		st = xmgd_sync();
+	if (st != XMG_OK) {
+		sp_free(sp);
+		return st;
+	}
+	*out = sp;
+	return XMG_OK;
+}
+
+/* Move c's staged blocks back: pagefile through the readers, host
+ * blocks straight into their pinned memory. */
+static int
+sp_commit(struct stream_plan *sp, xm_tensor_t *c)
+{
+	struct io_job j;
+
+	if (sp->ncw == 0)
+		return XMG_OK;
+	memset(&j, 0, sizeof j);
+	j.al = c->allocator;
+	j.h = sp->CH; j.sz = sp->CSZ; j.dst = sp->CD; j.n = sp->ncw; j.wr = 1;
+	int st = io_start(&j);
+	return st == XMG_OK ? io_join(&j) : st;
+}
+
+/*
+ * One call of a streamed contraction: a's (and, for beta != 0, c's)
+ * blocks and batch 0 are read while batch 0's plan is built (on the
+ * first call), then batch k + 1 streams into the idle region while batch
+ * k is contracted, and c is written back.  Batch plans missing from sp
+ * are cut from p0 (the whole plan) and kept in sp.
+ */
+static int
+sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
+{
+	struct batch_buf bb = {NULL, NULL, NULL, NULL, NULL, NULL};
+	struct io_job io[2];
+	uint64_t *JH = NULL, *JSZ = NULL, *JD = NULL;
+	xmg_hmap_t filt;
+	xmg_stats_t acc;
+	size_t i, k, n0 = sp->bstart[1];
+	double tw = 0;
+	int st = XMG_OK, used_all = XMG_PREC_EMU64;
+
 	memset(io, 0, sizeof io);
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;
-	acc.ms_plan = tp;
-	batch_buf_alloc(&bb, &p0);
 	xmg_hmap_init(&filt);
-	if ((*st = xmgd_alloc(rbytes, &reg[0])) != XMG_OK ||
-	    (nb > 1 && (*st = xmgd_alloc(rbytes, &reg[1])) != XMG_OK) ||
-	    (*st = xmgd_sync()) != XMG_OK)
-		goto out_free;
 	for (k = 0; k < 2; k++)
-		io[k].al = b->allocator;
-	/* every b block's address in its batch's region */
-	for (k = 0; k < nb; k++)
-		for (i = bstart[k]; i < bstart[k + 1]; i++)
-			D[i] = reg[k & 1] + OFF[i];
-	/* a's and c's blocks as views in one buffer, read together with
-	 * batch 0 while batch 0's plan is built (plans need addresses only) */
-	if ((*st = bulk_views(a, c, creal(beta) != 0 || cimag(beta) != 0, &VH,
-	    &VSZ, &VD, &nv)) != XMG_OK)
-		goto out_free;
-	JH = malloc((nv + bstart[1] + 1) * sizeof *JH);
-	JSZ = malloc((nv + bstart[1] + 1) * sizeof *JSZ);
-	JD = malloc((nv + bstart[1] + 1) * sizeof *JD);
+		io[k].al = sp->b->allocator;
+	JH = malloc((sp->nr + n0 + 1) * sizeof *JH);
+	JSZ = malloc((sp->nr + n0 + 1) * sizeof *JSZ);
+	JD = malloc((sp->nr + n0 + 1) * sizeof *JD);
 	if (!JH || !JSZ || !JD)
 		xm_fatal("%s: out of memory", __func__);
-	memcpy(JH, VH, nv * sizeof *JH);
-	memcpy(JSZ, VSZ, nv * sizeof *JSZ);
-	memcpy(JD, VD, nv * sizeof *JD);
-	memcpy(JH + nv, H, bstart[1] * sizeof *JH);
-	memcpy(JSZ + nv, SZ, bstart[1] * sizeof *JSZ);
-	memcpy(JD + nv, D, bstart[1] * sizeof *JD);
+	memcpy(JH, sp->RH, sp->nr * sizeof *JH);
+	memcpy(JSZ, sp->RSZ, sp->nr * sizeof *JSZ);
+	memcpy(JD, sp->RD, sp->nr * sizeof *JD);
+	memcpy(JH + sp->nr, sp->H, n0 * sizeof *JH);
+	memcpy(JSZ + sp->nr, sp->SZ, n0 * sizeof *JSZ);
+	memcpy(JD + sp->nr, sp->D, n0 * sizeof *JD);
 	io[0].h = JH; io[0].sz = JSZ; io[0].dst = JD;
-	io[0].n = nv + bstart[1];
-	if ((*st = io_start(&io[0])) != XMG_OK)
-		goto out_free;
-	tw = 0;
-	for (k = 0; k < nb && *st == XMG_OK; k++) {
+	io[0].n = sp->nr + n0;
+	if ((st = io_start(&io[0])) != XMG_OK)
+		goto out;
+	for (k = 0; k < sp->nb && st == XMG_OK; k++) {
 		struct io_job *nx = &io[(k + 1) & 1];
-		xmgd_contract_t dp;
-		xmgd_plan_t *hp = NULL;
 		int used = XMG_PREC_FP64;
 		double t0 = now_ms();
 
-		/* the batch's blocks resolve into its region */
-		xmg_hmap_free(&filt);
-		xmg_hmap_init(&filt);
-		for (i = bstart[k]; i < bstart[k + 1]; i++)
-			if (xmg_hmap_put(&filt, H[i], D[i]))
-				xm_fatal("%s: out of memory", __func__);
-		if ((*st = batch_plan(&p0, &filt, a->allocator, &bb, alpha,
-		    k == 0 ? beta : 1, prec, &dp)) == XMG_OK)
-			*st = xmgd_plan_create(&dp, &hp);
+		if (sp->bp[k] == NULL) {
+			xmgd_contract_t dp;
+			if (p0 == NULL) {
+				st = xmg_seterr(XMG_EINVAL, "xm_contract: streamed "
+				    "plan without its batch plans");
+				break;
+			}
+			if (bb.cb == NULL)
+				batch_buf_alloc(&bb, p0);
+			/* the batch's blocks resolve into its region */
+			xmg_hmap_free(&filt);
+			xmg_hmap_init(&filt);
+			for (i = sp->bstart[k]; i < sp->bstart[k + 1]; i++)
+				if (xmg_hmap_put(&filt, sp->H[i], sp->D[i]))
+					xm_fatal("%s: out of memory", __func__);
+			if ((st = batch_plan(p0, &filt, &sp->vmap, &bb, sp->alpha,
+			    k == 0 ? sp->beta : 1, sp->precision, &dp)) == XMG_OK) {
+				/* a kept plan is replayed: graphs and tuning */
+				dp.one_shot = !sp->keep;
+				st = xmgd_plan_create(&dp, &sp->bp[k]);
+				sp->bflops[k] = dp.flops;
+				sp->bnpairs[k] = dp.npairs;
+			}
+		}
 		acc.ms_plan += now_ms() - t0;
 		/* batch k's data in place (only batch 0 can still be loading:
 		 * later batches were joined at the end of the previous round),
@@ -1494,70 +1688,114 @@ contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
 			t0 = now_ms();
 			int s2 = io_join(&io[0]);
 			tw += now_ms() - t0;
-			if (*st == XMG_OK)
-				*st = s2;
+			if (st == XMG_OK)
+				st = s2;
 		}
-		if (*st == XMG_OK && k + 1 < nb) {
-			nx->h = H + bstart[k + 1];
-			nx->sz = SZ + bstart[k + 1];
-			nx->dst = D + bstart[k + 1];
-			nx->n = bstart[k + 2] - bstart[k + 1];
-			*st = io_start(nx);
+		if (st == XMG_OK && k + 1 < sp->nb) {
+			nx->h = sp->H + sp->bstart[k + 1];
+			nx->sz = sp->SZ + sp->bstart[k + 1];
+			nx->dst = sp->D + sp->bstart[k + 1];
+			nx->n = sp->bstart[k + 2] - sp->bstart[k + 1];
+			st = io_start(nx);
 		}
-		if (*st == XMG_OK)
-			*st = xmgd_plan_run(hp, &used);
-		if (hp)
-			xmgd_plan_free(hp);
-		if (*st == XMG_OK) {
+		if (st == XMG_OK)
+			st = xmgd_plan_run(sp->bp[k], &used);
+		if (st == XMG_OK) {
 			xmgd_timing_t tm;
 			xmgd_last_timing(&tm);
-			acc.flops += dp.flops;
+			acc.flops += sp->bflops[k];
 			acc.ms_device += tm.ms_total;
 			acc.ms_split += tm.ms_split;
 			acc.ms_gemm += tm.ms_gemm;
-			acc.n_pairs += dp.npairs;
+			acc.n_pairs += sp->bnpairs[k];
 			acc.gemm_launches += tm.gemm_launches;
 			acc.gemm_policy = tm.gemm_policy;
 			if (tm.slice_bytes > acc.slice_bytes)
 				acc.slice_bytes = tm.slice_bytes;
-			if (dp.npairs > 0 && used != XMG_PREC_EMU64)
+			if (sp->bnpairs[k] > 0 && used != XMG_PREC_EMU64)
 				used_all = XMG_PREC_FP64;
 		}
 		t0 = now_ms();
-		if (k + 1 < nb) {
+		if (k + 1 < sp->nb) {
 			int s2 = io_join(nx);
-			if (*st == XMG_OK)
-				*st = s2;
+			if (st == XMG_OK)
+				st = s2;
 		}
 		tw += now_ms() - t0;
 	}
 	for (k = 0; k < 2; k++)
 		io_join(&io[k]);	/* never leave a copy in flight */
-	acc.n_cblocks = 0;
-	{
-		xm_dim_t *list; size_t n;
-		xm_tensor_get_canonical_block_list(c, &list, &n);
-		acc.n_cblocks = (long long)n;
-		free(list);
-	}
+	if (st == XMG_OK)
+		st = sp_commit(sp, c);
+	acc.n_cblocks = sp->ncb;
 	acc.precision_used = used_all;
-	acc.stage_bytes = (long long)total;
-	acc.stage_batches = (int)nb;
+	acc.stage_bytes = (long long)sp->total;
+	acc.stage_batches = (int)sp->nb;
 	acc.ms_stage_wait = tw;
-	g_stats = acc;
-out_free:
-	xmg_hmap_free(&filt);
-	if (reg[0])
-		xmgd_free(reg[0]);
-	if (reg[1])
-		xmgd_free(reg[1]);
-	*st = commit_c(c, *st);
-	xmg_alloc_release_views(a->allocator, 0);
+	if (st == XMG_OK)
+		g_stats = acc;
 out:
-	plan_free(&p0);
+	xmg_hmap_free(&filt);
 	batch_buf_free(&bb);
-	free(u); free(H); free(SZ); free(OFF); free(D); free(bstart);
-	free(VH); free(VSZ); free(VD); free(JH); free(JSZ); free(JD);
+	free(JH); free(JSZ); free(JD);
+	return st;
+}
+
+/*
+ * Pagefile and host-memory path.  Returns 0 when the contraction should
+ * run through the in-core path (b in GPU memory or b aliasing a or c, no
+ * GEMMs, or a structure error that path reports), else 1 with the status
+ * in *st.  A pagefile b is streamed in batches when its blocks exceed the
+ * staging budget, else staged whole as a single batch; a host-memory b is
+ * always streamed.  The streamed plan of the last such contraction is
+ * kept (XMG_STREAM_CACHE=0 disables that) and reused by a matching call.
+ */
+static int
+contract_streamed(xm_scalar_t alpha, const xm_tensor_t *a,
+    const xm_tensor_t *b, xm_scalar_t beta, xm_tensor_t *c,
+    const char *idxa, const char *idxb, const char *idxc, int prec, int *st)
+{
+	struct stream_plan *sp = NULL;
+	plan_t p0;
+	const char *e = getenv("XMG_STREAM_CACHE");
+	const int cache = !(e && strcmp(e, "0") == 0);
+	double tp = now_ms();
+	int incore = 0;
+
+	if (xmg_alloc_is_device(b->allocator) || b == a || b == c)
+		return 0;
+	if (!g_stage_budget)
+		g_stage_budget = env_bytes("XMG_STAGE_BUDGET_GB", 180);
+	if (!g_stage_region)
+		g_stage_region = env_bytes("XMG_STAGE_REGION_GB", 32);
+	init_plan(&p0);
+	if (cache && sp_match(g_sp, alpha, a, b, beta, c, idxa, idxb, idxc,
+	    prec, g_stage_budget, g_stage_region)) {
+		sp = g_sp;
+		g_sp = NULL;
+	} else {
+		/* the kept plan's device memory goes before the new one's */
+		sp_free(g_sp);
+		g_sp = NULL;
+		*st = sp_build(alpha, a, b, beta, c, idxa, idxb, idxc, prec,
+		    g_stage_budget, g_stage_region, &p0, &sp, &incore);
+		if (incore) {
+			plan_free(&p0);
+			return 0;
+		}
+		if (*st != XMG_OK) {
+			plan_free(&p0);
+			return 1;
+		}
+	}
+	tp = now_ms() - tp;
+	*st = sp_run(sp, sp->bp[sp->nb - 1] ? NULL : &p0, c);
+	g_stats.ms_plan += tp;
+	plan_free(&p0);
+	if (*st == XMG_OK && cache && sp->keep)
+		g_sp = sp;
+	else
+		sp_free(sp);
 	return 1;
 }
 
@@ -1634,6 +1872,8 @@ xmg_plan_cache_clear(void)
 
 	for (i = 0; i < PC_MAX; i++)
 		pc_drop(&g_pc[i]);
+	sp_free(g_sp);
+	g_sp = NULL;
 }
 
 static void

@@ -335,6 +335,95 @@ xm_tensor_write_block(xm_tensor_t *t, xm_dim_t blkidx, const void *buf)
 	    buf, xm_tensor_get_block_bytes(t, blkidx));
 }
 
+/* index check without exiting (the xmg_ list calls return a status) */
+static int
+block_of(const xm_tensor_t *t, xm_dim_t blkidx, const char *fn,
+    struct xmg_block **out)
+{
+	xm_dim_t nb = xm_block_space_get_nblocks(t->bs);
+
+	if (blkidx.n != nb.n || !xm_dim_less(&blkidx, &nb))
+		return xmg_seterr(XMG_EINVAL, "%s: block index out of range", fn);
+	*out = &t->blocks[xm_dim_offset(&blkidx, &nb)];
+	return XMG_OK;
+}
+
+/*
+ * n blocks in one call.  For tensors in GPU memory every block's copy is
+ * queued on the engine stream (one cudaMemcpyAsync each) and the call
+ * waits once, at the end; the caller's buffers may be reused on return,
+ * as after xm_tensor_write_block.  Pagefile and host-memory tensors write
+ * block by block.
+ */
+int
+xmg_tensor_write_blocks(xm_tensor_t *t, size_t n, const xm_dim_t *blks,
+    const void *const *bufs)
+{
+	const char *fn = "xmg_tensor_write_blocks";
+	struct xmg_block *b;
+	size_t i;
+	int st = XMG_OK, s2;
+
+	if (t == NULL || (n > 0 && (blks == NULL || bufs == NULL)))
+		return xmg_seterr(XMG_EINVAL, "%s: NULL argument", fn);
+	for (i = 0; i < n; i++) {
+		if ((st = block_of(t, blks[i], fn, &b)) != XMG_OK)
+			return st;
+		if (b->type != XM_BLOCK_TYPE_CANONICAL)
+			return xmg_seterr(XMG_EINVAL, "%s: can only write to "
+			    "canonical blocks", fn);
+		if (bufs[i] == NULL)
+			return xmg_seterr(XMG_EINVAL, "%s: NULL buffer", fn);
+	}
+	for (i = 0; st == XMG_OK && i < n; i++) {
+		b = xmg_tensor_block(t, blks[i]);
+		size_t bytes = xm_tensor_get_block_bytes(t, blks[i]);
+		st = xmg_alloc_is_device(t->allocator) ?
+		    xmgd_h2d_async(b->data, bufs[i], bytes) :
+		    xmg_alloc_io(t->allocator, b->data, (void *)bufs[i], bytes, 1);
+	}
+	if (xmg_alloc_is_device(t->allocator) && n > 0 &&
+	    (s2 = xmgd_sync()) != XMG_OK && st == XMG_OK)
+		st = s2;
+	return st;
+}
+
+/* n nonzero blocks into n host buffers, the copies queued and waited for
+ * once as in xmg_tensor_write_blocks (derivative blocks read their
+ * source's data, as xm_tensor_read_block does) */
+int
+xmg_tensor_read_blocks(const xm_tensor_t *t, size_t n, const xm_dim_t *blks,
+    void *const *bufs)
+{
+	const char *fn = "xmg_tensor_read_blocks";
+	struct xmg_block *b;
+	size_t i;
+	int st = XMG_OK, s2;
+
+	if (t == NULL || (n > 0 && (blks == NULL || bufs == NULL)))
+		return xmg_seterr(XMG_EINVAL, "%s: NULL argument", fn);
+	for (i = 0; i < n; i++) {
+		if ((st = block_of(t, blks[i], fn, &b)) != XMG_OK)
+			return st;
+		if (b->type == XM_BLOCK_TYPE_ZERO)
+			return xmg_seterr(XMG_EINVAL, "%s: cannot read data from "
+			    "zero-blocks", fn);
+		if (bufs[i] == NULL)
+			return xmg_seterr(XMG_EINVAL, "%s: NULL buffer", fn);
+	}
+	for (i = 0; st == XMG_OK && i < n; i++) {
+		uint64_t h = xm_tensor_get_block_data_ptr(t, blks[i]);
+		size_t bytes = xm_tensor_get_block_bytes(t, blks[i]);
+		st = xmg_alloc_is_device(t->allocator) ?
+		    xmgd_d2h_async(bufs[i], h, bytes) :
+		    xmg_alloc_io(t->allocator, h, bufs[i], bytes, 0);
+	}
+	if (xmg_alloc_is_device(t->allocator) && n > 0 &&
+	    (s2 = xmgd_sync()) != XMG_OK && st == XMG_OK)
+		st = s2;
+	return st;
+}
+
 /*
  * Iteration space of an unfold: mask_i positions (first fastest) then
  * mask_j positions; matrix side offset i + stride * j; block side offset

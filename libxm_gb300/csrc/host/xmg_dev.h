@@ -26,6 +26,13 @@ int xmgd_is_device_ptr(const void *p);
 int xmgd_scratch(int slot, size_t bytes, uint64_t *dptr);
 /* Pinned host staging buffer (grow-only). */
 int xmgd_pinned(size_t bytes, void **hptr);
+/* Page-locked host memory for host-allocator blocks (on the GPU's
+ * nearest NUMA node where the system has several). */
+int xmgd_host_alloc(size_t bytes, void **hptr);
+void xmgd_host_free(void *p);
+/* Asynchronous copies on the engine stream (xmgd_sync waits). */
+int xmgd_h2d_async(uint64_t dst, const void *src, size_t bytes);
+int xmgd_d2h_async(void *dst, uint64_t src, size_t bytes);
 /* Out-of-core staging on the side stream: pinned chunk buffers in
  * XMGD_SIDE_SLOTS slots (two per reader thread); side_copy sends chunk
  * `slot` to dst asynchronously, side_fetch fills it from src, side_wait
@@ -39,6 +46,10 @@ int xmgd_side_copy(int slot, uint64_t dst, size_t bytes);
 int xmgd_side_fetch(int slot, uint64_t src, size_t bytes);
 int xmgd_side_wait(int slot);
 int xmgd_side_sync(void);
+/* Copies between page-locked host memory and HBM on the side stream,
+ * without a chunk slot (host-allocator blocks); xmgd_side_sync waits. */
+int xmgd_side_put(uint64_t dst, const void *src, size_t bytes);
+int xmgd_side_get(void *dst, uint64_t src, size_t bytes);
 size_t xmgd_arena_bytes_in_use(void);
 
 /* ---- permuted element-wise ops over blocks -------------------------- */

@@ -46,6 +46,8 @@ void xmg_tensor_touch(xm_tensor_t *t);
 
 /* allocator internals used by the contraction engine */
 int xmg_alloc_is_device(const xm_allocator_t *a);
+/* blocks in page-locked host memory (xmg_allocator_create_host) */
+int xmg_alloc_is_host(const xm_allocator_t *a);
 /* Device address holding the bytes of a data handle.  For pagefile
  * allocators the block is staged into an engine-owned HBM buffer first. */
 int xmg_alloc_device_view(xm_allocator_t *a, uint64_t handle, size_t bytes,
@@ -69,6 +71,8 @@ static inline void xmg_scalar_pack(xm_scalar_t s, double out[2])
 
 #endif /* XMG_HOST_H */
 
+int xmg_alloc_io(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes,
+    int wr);
 int xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
     void *mem, size_t bytes);
 int xmg_alloc_write_range(xm_allocator_t *a, uint64_t h, size_t byte_off,

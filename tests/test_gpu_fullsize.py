@@ -102,7 +102,7 @@ def test_adjoint_full_size(engine, oracle, ladder_pair):
     its multiplicity."""
     we, wo = ladder_pair
     alpha = 1.0
-    oal = api.Allocator(oracle)
+    oal = wo.a.alloc        # xm_contract wants one allocator for all three
     dce = we.c.structure()
     W.fill(dce, 77, W.LADDER_ANTISYM)
     da, db = we.a.structure(), we.b.structure()
@@ -126,7 +126,6 @@ def test_adjoint_full_size(engine, oracle, ladder_pair):
     rel_b = W.rel_frobenius(gdb, ref_db)
     for x in (da, db, dce, wt, dco):
         x.free()
-    oal.destroy()
     assert rel_a <= 1e-11, rel_a
     assert rel_b <= 1e-11, rel_b
     assert st.precision_used == api.PREC_EMU64
