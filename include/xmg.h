@@ -135,6 +135,13 @@ int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
     const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,
     xm_tensor_t *db, const char *idxa, const char *idxb, const char *idxc);
 
+/* For tensors in GPU memory the adjoint keeps its intermediates (W and the
+ * gradients at every nonzero position of a and b) and, through the plan
+ * cache, the device plans of its two contractions while a, b and dc keep
+ * their block structures, so that repeated calls neither plan nor
+ * allocate.  This frees them (xmg_plan_cache_clear does too). */
+void xmg_adjoint_release(void);
+
 /* Allocation-free dot product.  No counterpart in the reference: it is an
  * addition for callers that cannot allocate memory at the point where they
  * need the value -- typically a host program whose own pool already holds

@@ -131,6 +131,7 @@ _GB_SIGS = {
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
     "xmg_plan_cache_clear": (None, []),
+    "xmg_adjoint_release": (None, []),
     "xmg_set_staging": (C.c_int, [C.c_size_t, C.c_size_t]),
     "xmg_selftest_bounded_wait": (C.c_int, [C.c_uint]),
     "xmg_block_space_autosplit_tiles": (C.c_int, [_P, C.c_size_t, C.c_size_t]),

@@ -132,13 +132,37 @@ same_space(const xm_tensor_t *x, const xm_tensor_t *y)
 	    xm_block_space_eq(x->bs, y->bs);
 }
 
+/*
+ * The intermediates of the last adjoint call -- W and the two gradient
+ * tensors at every nonzero position -- are kept while a, b and dc keep
+ * their block structures (and so are the device plans of the two
+ * gradient contractions, which the plan cache keys on these tensors): a
+ * training-style loop that calls the adjoint every step plans and
+ * allocates once.  xmg_adjoint_release (and xmg_plan_cache_clear) frees
+ * them.
+ */
+static struct {
+	const xm_tensor_t *a, *b, *dc;
+	uint64_t ga_gen, gb_gen, gdc_gen;
+	xm_tensor_t *w, *ga, *gb;
+} g_adj;
+
+void
+xmg_adjoint_release(void)
+{
+	drop(g_adj.w);
+	drop(g_adj.ga);
+	drop(g_adj.gb);
+	memset(&g_adj, 0, sizeof g_adj);
+}
+
 int
 xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
     const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,
     xm_tensor_t *db, const char *idxa, const char *idxb, const char *idxc)
 {
 	xm_tensor_t *w = NULL, *ga = NULL, *gb = NULL;
-	int st;
+	int st, kept;
 
 	if (a == NULL || b == NULL || dc == NULL)
 		return xmg_seterr(XMG_EINVAL, "xm_contract_adjoint: invalid "
@@ -150,28 +174,54 @@ xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
 	if (a->type != dc->type || a->allocator != dc->allocator)
 		return xmg_seterr(XMG_EINVAL, "xm_contract_adjoint: dc must "
 		    "match the operands' type and allocator");
-	/* W: dc folded onto dc's own canonical positions (c and dc share
-	 * their block structure; the structure tensor here is dc) */
-	w = gradient_tensor(dc, 0);
+	kept = g_adj.w != NULL && g_adj.a == a && g_adj.b == b &&
+	    g_adj.dc == dc && g_adj.ga_gen == a->gen && g_adj.gb_gen == b->gen &&
+	    g_adj.gdc_gen == dc->gen && xmg_alloc_is_device(a->allocator);
+	if (!kept) {
+		xmg_adjoint_release();
+		/* W: dc folded onto dc's own canonical positions (c and dc
+		 * share their block structure; the structure tensor is dc) */
+		w = gradient_tensor(dc, 0);
+	} else
+		w = g_adj.w;
 	if ((st = xmg_set(w, 0)) != XMG_OK ||
 	    (st = fold_onto_canonical(dc, w, dc, 1)) != XMG_OK)
 		goto out;
 	if (da) {
-		ga = gradient_tensor(a, 1);
+		if ((ga = kept ? g_adj.ga : NULL) == NULL)
+			ga = gradient_tensor(a, 1);
 		if ((st = xmg_contract(alpha, w, b, 0, ga, idxc, idxb, idxa)) !=
 		    XMG_OK || (st = fold_onto_canonical(a, da, ga, 0)) != XMG_OK)
 			goto out;
 	}
 	if (db) {
-		gb = gradient_tensor(b, 1);
+		if ((gb = kept ? g_adj.gb : NULL) == NULL)
+			gb = gradient_tensor(b, 1);
 		if ((st = xmg_contract(alpha, a, w, 0, gb, idxa, idxc, idxb)) !=
 		    XMG_OK || (st = fold_onto_canonical(b, db, gb, 0)) != XMG_OK)
 			goto out;
 	}
 	st = xmgd_sync();
 out:
-	drop(w);
-	drop(ga);
-	drop(gb);
+	if (st == XMG_OK && xmg_alloc_is_device(a->allocator)) {
+		/* keep the intermediates for the next call */
+		g_adj.a = a; g_adj.b = b; g_adj.dc = dc;
+		g_adj.ga_gen = a->gen; g_adj.gb_gen = b->gen;
+		g_adj.gdc_gen = dc->gen;
+		g_adj.w = w;
+		if (ga)
+			g_adj.ga = ga;
+		if (gb)
+			g_adj.gb = gb;
+		return st;
+	}
+	if (w != g_adj.w)
+		drop(w);
+	if (ga != g_adj.ga)
+		drop(ga);
+	if (gb != g_adj.gb)
+		drop(gb);
+	if (st != XMG_OK)
+		xmg_adjoint_release();
 	return st;
 }

@@ -1874,6 +1874,7 @@ xmg_plan_cache_clear(void)
 		pc_drop(&g_pc[i]);
 	sp_free(g_sp);
 	g_sp = NULL;
+	xmg_adjoint_release();
 }
 
 static void

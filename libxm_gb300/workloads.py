@@ -209,6 +209,34 @@ def cfg2(lib, alloc, seed=2, scale=1, o_blocks=None, v_blocks=None, fill_data=Tr
     return w
 
 
+def split_sizes(lib, dim, tiles=None):
+    """Block sizes of one dimension of length dim as the library's
+    autosplit cuts it: xm_block_space_autosplit (tiles None, the
+    reference's rule) or, on the engine, xmg_block_space_autosplit_tiles
+    with tiles = (target, quantum)."""
+    bs = api.BlockSpace(lib, [dim])
+    if tiles is None:
+        bs.autosplit()
+    else:
+        lib.check(lib.xmg_block_space_autosplit_tiles(bs.h, tiles[0], tiles[1]))
+    n = bs.nblocks()[0]
+    cuts = [lib.xm_block_space_get_split(bs.h, 0, i) for i in range(n + 1)]
+    bs.free()
+    return [cuts[i + 1] - cuts[i] for i in range(n)]
+
+
+def autosplit_ladder(lib, alloc, o_sizes, v_sizes, seed=4):
+    """A Z2^3-sparse ladder on given block sizes (labels from the uneven
+    ladder's seeds, one per block), for comparing block splittings of the
+    same dimensions."""
+    _, _, lo, lv = cfg2_shape(seed)
+    lo = (lo * 4)[:len(o_sizes)]
+    lv = (lv * 4)[:len(v_sizes)]
+    w = ladder(lib, alloc, o_sizes, v_sizes, seed, z2=(lo, lv))
+    w.name = "ladder_o%d_v%d_z2" % (sum(o_sizes), sum(v_sizes))
+    return w
+
+
 def cfg5_shape(seed=5):
     o = [16] * 8
     v = uneven_sizes(1024, 32, 24, 40, seed * 7 + 12)

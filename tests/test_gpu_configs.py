@@ -140,3 +140,62 @@ def test_adjoint_ladder(engine, oracle):
         x.free()
     we.free()
     wo.free()
+
+
+@pytest.mark.parametrize("dims,tiles", [((44, 92), (16, 8)), ((92, 188), (32, 16))])
+def test_tile_autosplit_ladder(engine, oracle, dims, tiles):
+    """A Z2^3 ladder on the opt-in tile-aware autosplit's blocks
+    (xmg_block_space_autosplit_tiles, every block a multiple of the
+    quantum but the last) against the oracle on the same splits, in both
+    precision modes."""
+    o_sz = W.split_sizes(engine, dims[0], tiles)
+    v_sz = W.split_sizes(engine, dims[1], tiles)
+    assert sum(o_sz) == dims[0] and sum(v_sz) == dims[1]
+    assert all(x % tiles[1] == 0 for x in o_sz[:-1] + v_sz[:-1])
+    eal, oal = api.Allocator(engine), api.Allocator(oracle)
+    we = W.autosplit_ladder(engine, eal, o_sz, v_sz)
+    wo = W.autosplit_ladder(oracle, oal, o_sz, v_sz)
+    wo.run()
+    ref = W.read_canonical(wo.c)
+    try:
+        for prec in (api.PREC_AUTO, api.PREC_FP64):
+            engine.check(engine.xmg_set_precision(prec))
+            we.run()
+            assert W.rel_frobenius(W.read_canonical(we.c), ref) <= 1e-12, prec
+    finally:
+        engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+        we.free()
+        wo.free()
+
+
+def test_adjoint_kept_intermediates(engine):
+    """Repeated adjoint calls reuse W, the gradient tensors and the plans of
+    the two gradient contractions: a call after new dC data equals the same
+    call computed from scratch (after xmg_adjoint_release)."""
+    al = api.Allocator(engine)
+    w = W.cfg2(engine, al, scale=4)
+    dc = w.c.structure()
+    da, db = w.a.structure(), w.b.structure()
+
+    def grads():
+        api.set_all(da, 0)
+        api.set_all(db, 0)
+        engine.check(engine.xm_contract_adjoint(api.Scalar.of(0.5), w.a.h, w.b.h, dc.h,
+                                                da.h, db.h, b"ijcd", b"cdab", b"ijab"))
+        return {**{("a",) + k: v for k, v in W.read_canonical(da).items()},
+                **{("b",) + k: v for k, v in W.read_canonical(db).items()}}
+    try:
+        W.fill(dc, 77, W.LADDER_ANTISYM)
+        g1 = grads()
+        W.fill(dc, 78, W.LADDER_ANTISYM)          # same structure, new data
+        g2 = grads()
+        engine.xmg_adjoint_release()
+        g3 = grads()
+        assert W.rel_frobenius(g2, g3) <= 1e-13
+        assert W.rel_frobenius(g1, g3) > 1e-3
+    finally:
+        engine.xmg_adjoint_release()
+        for x in (dc, da, db):
+            x.free()
+        w.free()
+        al.destroy()
