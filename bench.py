@@ -539,20 +539,20 @@ def engine_arm(args, ranks):
             p = eng.xmg_host_alloc(n)
             outs[blk] = (p, n)
             nbytes_out += n
-        lists = [(t, t.canonical_blocks()) for t in (w.a, w.b)]
-        ptrs = [[host[(id(t), blk)][0] for blk in blks] for t, blks in lists]
-        cblocks = list(outs)
-        cptrs = [outs[blk][0] for blk in cblocks]
+        lists = [(t, api.BlockList(t.canonical_blocks(),
+                                   [host[(id(t), blk)][0] for blk in t.canonical_blocks()]))
+                 for t in (w.a, w.b)]
+        cblocks = api.BlockList(list(outs), [outs[blk][0] for blk in outs])
         phase = np.zeros(3)
 
         def hbm_step():
             t0 = time.perf_counter()
-            for (t, blks), pp in zip(lists, ptrs):
-                t.write_blocks(blks, pp)
+            for t, bl in lists:
+                t.write_blocks(bl)
             t1 = time.perf_counter()
             w.run()
             t2 = time.perf_counter()
-            w.c.read_blocks(cblocks, cptrs)
+            w.c.read_blocks(cblocks)
             phase[:] += (t1 - t0, t2 - t1, time.perf_counter() - t2)
         hbm_step()
         ranks.barrier()
@@ -570,7 +570,7 @@ def engine_arm(args, ranks):
                     "(xmg_tensor_read_blocks) every step",
             "phases_ms": {"h2d": phase[0] * 1e3 / steps, "contract": phase[1] * 1e3 / steps,
                           "d2h": phase[2] * 1e3 / steps},
-            "copies_per_step": sum(len(b) for _, b in lists) + len(cblocks)}
+            "copies_per_step": sum(bl.n for _, bl in lists) + cblocks.n}
         for p, _ in host.values():
             eng.xmg_host_free(p)
         for p, _ in outs.values():

@@ -222,6 +222,16 @@ class Allocator:
             self.h = None
 
 
+class BlockList:
+    """The C arrays of a block list call (block indices, host addresses),
+    built once for calls that repeat."""
+
+    def __init__(self, blocks, ptrs):
+        self.n = len(blocks)
+        self.dims = (Dim * max(1, self.n))(*[Dim.of(b) for b in blocks])
+        self.bufs = (C.c_void_p * max(1, self.n))(*ptrs)
+
+
 class Tensor:
     def __init__(self, lib, bs, dtype, alloc, canonical=False, handle=None):
         self.lib = lib
@@ -293,19 +303,17 @@ class Tensor:
         self.lib.xm_tensor_read_block(self.h, Dim.of(blk), a.ctypes.data)
         return a
 
-    def write_blocks(self, blocks, ptrs):
-        """xmg_tensor_write_blocks: blocks[i] from the host address ptrs[i]."""
-        n = len(blocks)
-        dims = (Dim * max(1, n))(*[Dim.of(b) for b in blocks])
-        bufs = (C.c_void_p * max(1, n))(*ptrs)
-        self.lib.check(self.lib.xmg_tensor_write_blocks(self.h, n, dims, bufs))
+    def write_blocks(self, blocks, ptrs=None):
+        """xmg_tensor_write_blocks: blocks[i] from the host address ptrs[i]
+        (or a prepared BlockList)."""
+        bl = blocks if isinstance(blocks, BlockList) else BlockList(blocks, ptrs)
+        self.lib.check(self.lib.xmg_tensor_write_blocks(self.h, bl.n, bl.dims, bl.bufs))
 
-    def read_blocks(self, blocks, ptrs):
-        """xmg_tensor_read_blocks: blocks[i] into the host address ptrs[i]."""
-        n = len(blocks)
-        dims = (Dim * max(1, n))(*[Dim.of(b) for b in blocks])
-        bufs = (C.c_void_p * max(1, n))(*ptrs)
-        self.lib.check(self.lib.xmg_tensor_read_blocks(self.h, n, dims, bufs))
+    def read_blocks(self, blocks, ptrs=None):
+        """xmg_tensor_read_blocks: blocks[i] into the host address ptrs[i]
+        (or a prepared BlockList)."""
+        bl = blocks if isinstance(blocks, BlockList) else BlockList(blocks, ptrs)
+        self.lib.check(self.lib.xmg_tensor_read_blocks(self.h, bl.n, bl.dims, bl.bufs))
 
     def get_element(self, idx):
         return self.lib.xm_tensor_get_element(self.h, Dim.of(idx)).value()

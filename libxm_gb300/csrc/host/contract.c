@@ -1144,16 +1144,19 @@ distinct_b(const plan_t *p, struct hsz **out)
 	return nu;
 }
 
-/* b's blocks (distinct, in file order) in batches of at most `region`
- * bytes, each block at a STAGE_ALIGN-aligned offset of its batch: batch k
- * holds blocks bstart[k] .. bstart[k + 1] - 1 (bstart[nb] = nu), block i
- * at offset off[i]; *rbytes is the largest batch.  A block larger than the
- * region alone is an error. */
+/* b's blocks (distinct, in file order) in batches, each block at a
+ * STAGE_ALIGN-aligned offset of its batch: batch k holds blocks bstart[k]
+ * .. bstart[k + 1] - 1 (bstart[nb] = nu), block i at offset off[i];
+ * *rbytes is the largest batch.  Batch k takes at most cap_k bytes, with
+ * cap_k = region when first <= 0, else min(region, first * growth^k); a
+ * block larger than cap_k (but within the region) makes a batch of its
+ * own.  A block larger than the region is an error. */
 static int
-form_batches(const struct hsz *u, size_t nu, size_t region, uint64_t *off,
-    size_t *bstart, size_t *nb, uint64_t *rbytes)
+form_batches(const struct hsz *u, size_t nu, size_t region, double first,
+    double growth, uint64_t *off, size_t *bstart, size_t *nb, uint64_t *rbytes)
 {
 	uint64_t run = 0;
+	double cap = first > 0 && first < (double)region ? first : (double)region;
 	size_t i;
 
 	*nb = 0;
@@ -1164,7 +1167,12 @@ form_batches(const struct hsz *u, size_t nu, size_t region, uint64_t *off,
 			return xmg_seterr(XMG_ENOMEM, "xm_contract: a block of b "
 			    "(%llu bytes) exceeds the staging region (%zu bytes)",
 			    (unsigned long long)u[i].sz, region);
-		if (i == 0 || run + al > region) {
+		if (i == 0 || (run > 0 && (double)(run + al) > cap)) {
+			if (i > 0 && first > 0) {
+				cap *= growth;
+				if (cap > (double)region)
+					cap = (double)region;
+			}
 			bstart[(*nb)++] = i;
 			run = 0;
 		}
@@ -1311,8 +1319,8 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 	if (region > 0) {
 		/* the streamed path's batches of at most `region` bytes: each
 		 * block inside the region, aligned, after the previous one */
-		if ((st = form_batches(u, nu, (size_t)region, off, bstart, &nb,
-		    &rbytes)) != XMG_OK)
+		if ((st = form_batches(u, nu, (size_t)region, 0, 1, off, bstart,
+		    &nb, &rbytes)) != XMG_OK)
 			goto done;
 		if (nu > 0 && (bstart[0] != 0 || bstart[nb] != nu ||
 		    rbytes > (uint64_t)region))
@@ -1475,19 +1483,25 @@ sp_match(const struct stream_plan *sp, xm_scalar_t alpha,
 	    strcmp(sp->idx[2], idxc) == 0;
 }
 
-/* host-allocator b: batches of about total / XMG_HOST_BATCHES bytes (at
- * most `region`), so that the copies of one batch overlap the kernels of
- * the previous one */
-static size_t
-host_region(uint64_t total, size_t nu, size_t region)
+/* host-allocator b: about XMG_HOST_BATCHES (default 8) batches growing
+ * geometrically by XMG_HOST_GROWTH (default 1.2) per batch: the small
+ * first batch is the only copy nothing overlaps, and a batch's kernels
+ * (for the FP64 ladders about 5-6 ms per GB of b) outlast the copy of the
+ * next one (4.7 ms per GB over a 212 GB/s link) while the growth stays
+ * below their ratio.  Returns the first batch's byte budget. */
+static double
+host_first_batch(uint64_t total, double *growth)
 {
-	const char *e = getenv("XMG_HOST_BATCHES");
-	uint64_t nb = e ? (uint64_t)atoi(e) : 4, r;
+	const char *e = getenv("XMG_HOST_BATCHES"), *g = getenv("XMG_HOST_GROWTH");
+	double n = e ? atof(e) : 8, r = g ? atof(g) : 1.2;
 
-	if (nb < 1)
-		nb = 1;
-	r = (total + nb - 1) / nb + (uint64_t)STAGE_ALIGN * (nu / nb + 2);
-	return r < region ? (size_t)r : region;
+	if (n < 1)
+		n = 1;
+	if (!(r >= 1.0))
+		r = 1.0;
+	*growth = r;
+	return r > 1.0 ? (double)total * (r - 1) / (pow(r, n) - 1) :
+	    (double)total / n;
 }
 
 /*
@@ -1545,8 +1559,9 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		sp->total += u[i].sz;
 	/* within the budget a pagefile b is staged whole: one batch, still
 	 * read by the parallel readers; a host b is always streamed */
+	double first = 0, growth = 1;
 	if (xmg_alloc_is_host(b->allocator))
-		region = host_region(sp->total, sp->nu, region);
+		first = host_first_batch(sp->total, &growth);
 	else if (sp->total <= budget)
 		region = sp->total + sp->nu * STAGE_ALIGN;
 	sp->H = malloc(sp->nu * sizeof *sp->H);
@@ -1560,8 +1575,8 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		sp->H[i] = u[i].h;
 		sp->SZ[i] = u[i].sz;
 	}
-	st = form_batches(u, sp->nu, region, OFF, sp->bstart, &sp->nb,
-	    &sp->rbytes);
+	st = form_batches(u, sp->nu, region, first, growth, OFF, sp->bstart,
+	    &sp->nb, &sp->rbytes);
 	free(u);
 	if (st == XMG_OK) {
 		sp->bp = calloc(sp->nb, sizeof *sp->bp);
