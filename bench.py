@@ -522,23 +522,26 @@ def engine_arm(args, ranks):
         eng.xmg_plan_cache_clear()
         hal.destroy()
 
-        # (2) HBM tensors, block list calls from / into pinned buffers
-        host = {}
-        nbytes_in = nbytes_out = 0
+        # (2) HBM tensors, block list calls from / into pinned buffers (one
+        # page-locked buffer for the inputs, one for the outputs)
+        nbytes_in = sum(t.block_size(blk) for t in (w.a, w.b)
+                        for blk in t.canonical_blocks()) * 8
+        nbytes_out = sum(w.c.block_size(blk) for blk in w.c.canonical_blocks()) * 8
+        pin_in, pin_out = eng.xmg_host_alloc(nbytes_in), eng.xmg_host_alloc(nbytes_out)
+        host, outs, off = {}, {}, 0
         for t in (w.a, w.b):
             for blk in t.canonical_blocks():
                 n = t.block_size(blk) * 8
-                p = eng.xmg_host_alloc(n)
-                buf = np.frombuffer((api.C.c_char * n).from_address(p), dtype=np.float64)
+                buf = np.frombuffer((api.C.c_char * n).from_address(pin_in + off),
+                                    dtype=np.float64)
                 buf[:] = t.read_block(blk)
-                host[(id(t), blk)] = (p, buf)
-                nbytes_in += n
-        outs = {}
+                host[(id(t), blk)] = (pin_in + off, buf)
+                off += n
+        off = 0
         for blk in w.c.canonical_blocks():
             n = w.c.block_size(blk) * 8
-            p = eng.xmg_host_alloc(n)
-            outs[blk] = (p, n)
-            nbytes_out += n
+            outs[blk] = (pin_out + off, n)
+            off += n
         lists = [(t, api.BlockList(t.canonical_blocks(),
                                    [host[(id(t), blk)][0] for blk in t.canonical_blocks()]))
                  for t in (w.a, w.b)]
@@ -571,10 +574,8 @@ def engine_arm(args, ranks):
             "phases_ms": {"h2d": phase[0] * 1e3 / steps, "contract": phase[1] * 1e3 / steps,
                           "d2h": phase[2] * 1e3 / steps},
             "copies_per_step": sum(bl.n for _, bl in lists) + cblocks.n}
-        for p, _ in host.values():
-            eng.xmg_host_free(p)
-        for p, _ in outs.values():
-            eng.xmg_host_free(p)
+        eng.xmg_host_free(pin_in)
+        eng.xmg_host_free(pin_out)
 
     # out-of-core: the same contraction with every tensor in a host pagefile
     # and b streamed through two 2 GB HBM regions (reader threads, pinned

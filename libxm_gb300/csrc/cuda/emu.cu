@@ -35,7 +35,8 @@
  *     warp 0 streams stages with cp.async.bulk, warp 1 issues the slice
  *     products per 16-wide K step with tcgen05.mma.kind::f16 (bf16 x bf16 ->
  *     fp32) into TMEM accumulators, warps 2..17 drain them every 160 K
- *     elements (the exact groups stay below 3 * 160 * 2^14 < 2^23) into
+ *     elements for FP64 and every <= 336 for FP32 (the exact groups stay
+ *     below 3 * 336 * 2^14 < 2^24, exact in fp32) into
  *     per-thread int64 fixed-point sums in units of 2^(-16-F), applying the
  *     pair factor exactly.  The epilogue is the only FP64 work:
  *     C = alpha * 2^(eA + eB - 2 * EXPOFF - 16 - F) * V + beta * C, scattered
@@ -58,7 +59,8 @@ namespace xmg {
 
 constexpr int EMU_TM = 128;              /* rows per tile, both operands */
 constexpr int EMU_KS = 16;               /* K per stage = K per MMA */
-constexpr int EMU_CHUNK = 10;            /* K steps per exact chunk (160) */
+constexpr int EMU_CHUNK = 10;            /* K steps per chunk, FP64 (160) */
+constexpr int EMU_CHUNK32 = 21;          /* K steps per chunk at most, FP32 */
 constexpr int SLICE_BYTES = EMU_TM * EMU_KS * 2;          /* 4096 */
 #ifndef EMU_DW
 #define EMU_DW 16                        /* drain warps: 8 or 16 */
@@ -368,10 +370,21 @@ struct stage_cfg {
 };
 
 /* K steps [c0, c1) of the next chunk: chunks never straddle the re/im
- * boundary of a realified complex view */
+ * boundary of a realified complex view.  An exact group g accumulates at
+ * most 3 products of |d_p d_q| <= 2^14 per K element, so its integer sum
+ * stays below 2^24 (exact in fp32) for chunks of up to 341 elements.
+ * FP64 keeps 160 (its rounded low band's error grows with the chunk);
+ * FP32, all exact, takes up to 21 steps (336), the steps left split into
+ * equal chunks (32 steps: 16 + 16, not 21 + 11). */
+template <int S>
 __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 {
 	const int lim = (cplx && c0 < nks / 2) ? nks / 2 : nks;
+	if constexpr (S == fin<float>::S) {
+		const int left = lim - c0;
+		const int n = (left + EMU_CHUNK32 - 1) / EMU_CHUNK32;
+		return c0 + (left + n - 1) / n;
+	}
 	return min(lim, c0 + EMU_CHUNK);
 }
 
@@ -696,7 +709,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
 					const int nks = vb[pr.bview].n_ks;
 					for (int c0 = 0; c0 < nks && !s_err; ) {
-						const int c1 = chunk_end(c0, nks, cplx);
+						const int c1 = chunk_end<S>(c0, nks, cplx);
 						/* head: the first H (staged) steps; tail: the last T
 						 * steps; middle: the rest.  H, T <= hmax <= NST: the
 						 * stages a head or tail holds are released only after
@@ -705,7 +718,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						const int H = min(hmax, c1 - c0);
 						const int T = min(hmax, c1 - c0 - H);
 						/* every accumulator restarts each chunk: the exact
-						 * groups for their 2^23 bound, the low band because
+						 * groups for their 2^24 bound, the low band because
 						 * the tensor core's fp32 accumulation error grows
 						 * with the accumulation length (per-pair
 						 * accumulation measured 10x larger error) */
@@ -883,7 +896,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					esh[g] = pg.eshift;
 				}
 				for (int c0 = 0; c0 < nks; ) {
-					const int c1 = chunk_end(c0, nks, cplx);
+					const int c1 = chunk_end<S>(c0, nks, cplx);
 					/* each segment's pair factor sign * 2^shift (shift 0
 					 * or 1, checked by the planner) rides on the exact
 					 * fp32 -> int scales; the real pass negates the im * im
@@ -965,11 +978,12 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						tmem_wait_ld();
 #pragma unroll
 						for (int c = 0; c < 4; c++) {
-							/* exact integers: |i0| <= 2^22.4, |i1| <= 2^23.4,
-							 * |i0 * 256 + i1| < 2^31 */
+							/* exact integers: with the pair factor's 2^1,
+							 * |i0| <= 2^14 * 336 * 2 < 2^23.4 and |i1| <
+							 * 2^24.4; the packing is 64-bit */
 							int i0 = __float2int_rn(a0[c] * sa);
 							int i1 = __float2int_rn(a1[c] * sb);
-							long long d = (long long)(i0 * 256 + i1) << 8;
+							long long d = ((long long)i0 * 256 + i1) << 8;
 							if (LOW)
 								d += __float2int_rn(a2[c] * sc);
 							V[b4 * 4 + c] += d << F;

@@ -8,6 +8,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace xmg {
@@ -345,19 +347,55 @@ xmg_device_memory(size_t *free_bytes, size_t *total_bytes)
 	return XMG_OK;
 }
 
+/*
+ * Page-locked host memory for host-allocator blocks, carved from slabs of
+ * at least 1 GiB (one cudaHostAlloc each) with 256-byte aligned bump
+ * allocation: the copy engine reads a few large pinned regions much
+ * faster than thousands of separately pinned block-sized ones.  A slab
+ * keeps a count of its live blocks; when it drops to zero the slab is
+ * freed (the newest one is kept and reused from its start).
+ */
+struct slab { char *p; size_t n, used; long live; };
+static std::vector<slab> g_slabs;
+static const size_t SLAB_BYTES = (size_t)1 << 30;
+
 extern "C" int
 xmgd_host_alloc(size_t bytes, void **hptr)
 {
-	XMG_CK(cudaSetDevice(g_dev));
-	XMG_CK(cudaHostAlloc(hptr, bytes, cudaHostAllocDefault));
+	const size_t need = (bytes + 255) & ~(size_t)255;
+
+	if (g_slabs.empty() || g_slabs.back().n - g_slabs.back().used < need) {
+		slab s = {nullptr, need > SLAB_BYTES ? need : SLAB_BYTES, 0, 0};
+		XMG_CK(cudaSetDevice(g_dev));
+		XMG_CK(cudaHostAlloc((void **)&s.p, s.n, cudaHostAllocDefault));
+		g_slabs.push_back(s);
+	}
+	slab &s = g_slabs.back();
+	*hptr = s.p + s.used;
+	s.used += need;
+	s.live++;
 	return XMG_OK;
 }
 
 extern "C" void
 xmgd_host_free(void *p)
 {
-	if (p)
-		cudaFreeHost(p);
+	if (!p)
+		return;
+	for (size_t i = 0; i < g_slabs.size(); i++) {
+		slab &s = g_slabs[i];
+		if ((char *)p < s.p || (char *)p >= s.p + s.n)
+			continue;
+		if (--s.live > 0)
+			return;
+		if (i + 1 == g_slabs.size()) {
+			s.used = 0;	/* the newest slab is reused */
+			return;
+		}
+		cudaFreeHost(s.p);
+		g_slabs.erase(g_slabs.begin() + (long)i);
+		return;
+	}
 }
 
 extern "C" void *

@@ -156,6 +156,15 @@ xmg_adjoint_release(void)
 	memset(&g_adj, 0, sizeof g_adj);
 }
 
+/* The kept intermediates live in the operands' allocator: its
+ * destruction releases them first (xm_allocator_destroy). */
+void
+xmg_adjoint_forget(const xm_allocator_t *al)
+{
+	if (g_adj.w != NULL && g_adj.w->allocator == al)
+		xmg_adjoint_release();
+}
+
 int
 xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
     const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,

@@ -421,6 +421,7 @@ xm_allocator_destroy(xm_allocator_t *a)
 
 	if (a == NULL)
 		return;
+	xmg_adjoint_forget(a);
 	if (a->path != NULL) {
 		xmg_alloc_release_views(a, 0);
 		if (close(a->fd))

@@ -758,6 +758,7 @@ struct io_job {
 	char err[256];
 	pthread_t th;
 	int running;
+	double ms;               /* wall time of the job (start to drained) */
 };
 
 /* one reader: chunks w, w + nw, w + 2 nw, ... of the list, alternating
@@ -844,6 +845,8 @@ io_host(struct io_job *j)
 	j->status = st;
 }
 
+static double now_ms(void);
+
 static void *
 io_main(void *arg)
 {
@@ -851,9 +854,11 @@ io_main(void *arg)
 	struct io_worker r[XMGD_SIDE_SLOTS / 2];
 	pthread_t th[XMGD_SIDE_SLOTS / 2];
 	int nw = stage_threads(), w, started = 0, st = XMG_OK;
+	double t0 = now_ms();
 
 	if (xmg_alloc_is_host(j->al)) {
 		io_host(j);
+		j->ms = now_ms() - t0;
 		return NULL;
 	}
 
@@ -883,6 +888,7 @@ io_main(void *arg)
 		snprintf(j->err, sizeof j->err, "%s", xmg_last_error());
 	}
 	j->status = st;
+	j->ms = now_ms() - t0;
 	return NULL;
 }
 
@@ -1644,6 +1650,9 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 	double tw = 0;
 	int st = XMG_OK, used_all = XMG_PREC_EMU64;
 
+	const char *tr = getenv("XMG_STREAM_TRACE");
+	const int trace = tr && strcmp(tr, "0") != 0;
+
 	memset(io, 0, sizeof io);
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;
@@ -1713,8 +1722,10 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 			nx->n = sp->bstart[k + 2] - sp->bstart[k + 1];
 			st = io_start(nx);
 		}
+		double tr0 = now_ms(), tw0 = tw;
 		if (st == XMG_OK)
 			st = xmgd_plan_run(sp->bp[k], &used);
+		const double trun = now_ms() - tr0;
 		if (st == XMG_OK) {
 			xmgd_timing_t tm;
 			xmgd_last_timing(&tm);
@@ -1737,9 +1748,21 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 				st = s2;
 		}
 		tw += now_ms() - t0;
+		if (trace) {
+			uint64_t bytes = 0;
+			for (i = sp->bstart[k]; i < sp->bstart[k + 1]; i++)
+				bytes += sp->SZ[i];
+			fprintf(stderr, "xmg stream: batch %zu/%zu %.3f GB, run %.2f "
+			    "ms, next batch's copy %.2f ms, waits %.2f ms\n", k,
+			    sp->nb, bytes / 1e9, trun, k + 1 < sp->nb ? nx->ms : 0.0,
+			    tw - tw0);
+		}
 	}
 	for (k = 0; k < 2; k++)
 		io_join(&io[k]);	/* never leave a copy in flight */
+	if (trace)
+		fprintf(stderr, "xmg stream: a, c and batch 0 copied in %.2f ms\n",
+		    io[0].ms);
 	if (st == XMG_OK)
 		st = sp_commit(sp, c);
 	acc.n_cblocks = sp->ncb;

@@ -44,6 +44,9 @@ struct xm_tensor {
 /* new structure generation for t (block table changed) */
 void xmg_tensor_touch(xm_tensor_t *t);
 
+/* release the adjoint's kept intermediates if they live in `al` */
+void xmg_adjoint_forget(const xm_allocator_t *al);
+
 /* allocator internals used by the contraction engine */
 int xmg_alloc_is_device(const xm_allocator_t *a);
 /* blocks in page-locked host memory (xmg_allocator_create_host) */

@@ -166,7 +166,7 @@ def test_block_list_calls(engine, hal, where):
     """xmg_tensor_write_blocks / read_blocks round trip, against the
     one-block calls, and their argument checks."""
     al = api.Allocator(engine) if where == "gpu" else hal
-    w = W.cfg1(engine, al)
+    w = W.cfg2(engine, al, scale=4)          # zero, canonical and derivative blocks
     try:
         blocks = w.b.canonical_blocks()
         data = [W.uniform(200 + i, w.b.block_size(blk)) for i, blk in enumerate(blocks)]
