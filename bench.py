@@ -55,6 +55,12 @@ def parse():
     p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
     p.add_argument("--subset", type=str, default=None,
                    help="O,V: keep the first O occupied and V virtual blocks (profiling case)")
+    p.add_argument("--cfg5-v-blocks", type=int, default=12,
+                   help="v blocks of the production ladder's structure streamed from a pagefile")
+    p.add_argument("--cfg5-region-gb", type=float, default=2.0,
+                   help="HBM region size for that measurement")
+    p.add_argument("--cfg5-only", action="store_true",
+                   help="only the production-ladder subset measurement (one JSON line)")
     return p.parse_args()
 
 
@@ -363,40 +369,46 @@ def tile_autosplit(eng, api, W, al):
     return res
 
 
-def cfg5_subset(eng, api, W, v_blocks=12):
+def cfg5_subset(eng, api, W, v_blocks=12, region=int(2e9)):
     """The production ladder's structure (o = 128 as 8 x 16, v blocks of
     24..40 with Z2^3 labels) on its first v_blocks v blocks, all tensors in
-    a pagefile and b streamed through two 2 GB regions: split-precision
-    against the plain FP64 path on the same inputs, wall clock per
-    xm_contract.  The full b (~275 GB) exceeds the host's disk and RAM."""
+    a pagefile and b streamed through two HBM regions of `region` bytes:
+    split-precision against the plain FP64 path on the same inputs, wall
+    clock per xm_contract (the first split-precision call plans; the
+    repeated ones reuse the kept streamed plan).  The full b (~275 GB)
+    exceeds the host's disk and RAM."""
     import tempfile
     tmp = tempfile.mkdtemp(prefix="xmg_cfg5_")
     pal = api.Allocator(eng, os.path.join(tmp, "pagefile"))
     t0 = time.perf_counter()
-    w = W.cfg5(eng, pal, v_blocks=v_blocks)
+    w = W.cfg5(eng, pal, v_blocks=v_blocks, threads=os.cpu_count() or 1)
     setup = time.perf_counter() - t0
     fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(),
                                 w.idxc.encode())
     nb = sum(w.b.block_size(blk) for blk in w.b.canonical_blocks()) * 8
     out = {"workload": w.name, "v_blocks": v_blocks, "b_bytes": nb, "useful_flops": fl,
-           "setup_s": setup}
-    eng.check(eng.xmg_set_staging(1, int(2e9)))
+           "region_bytes": region, "setup_s": setup}
+    eng.check(eng.xmg_set_staging(1, region))
     try:
         res = {}
         for prec, name, reps in ((api.PREC_AUTO, "emu", 2), (api.PREC_FP64, "fp64", 1)):
             eng.check(eng.xmg_set_precision(prec))
+            plan_ms = []
             if prec == api.PREC_AUTO:
                 w.run()
+                plan_ms.append(api.last_stats(eng).ms_plan)
             best = 1e30
             for _ in range(reps):
                 t0 = time.perf_counter()
                 w.run()
                 best = min(best, time.perf_counter() - t0)
+                plan_ms.append(api.last_stats(eng).ms_plan)
             st = api.last_stats(eng)
             res[name] = W.read_canonical(w.c)
             out[name] = {"ms": best * 1e3, "tflops": fl / best / 1e12,
                          "device_ms": st.ms_device, "batches": st.stage_batches,
                          "stage_gbs": st.stage_bytes / best / 1e9,
+                         "stage_wait_ms": st.ms_stage_wait, "plan_ms": plan_ms,
                          "precision_used": "emu64" if st.precision_used == api.PREC_EMU64
                          else "fp64"}
         out["speedup_vs_fp64_plain"] = out["fp64"]["ms"] / out["emu"]["ms"]
@@ -436,6 +448,11 @@ def engine_arm(args, ranks):
     from libxm_gb300 import api, workloads as W
     libxm_gb300.build()
     eng = libxm_gb300.load()
+    if args.cfg5_only:
+        if ranks.rank == 0:
+            print(json.dumps({"cfg5_subset": cfg5_subset(
+                eng, api, W, args.cfg5_v_blocks, int(args.cfg5_region_gb * 1e9))}))
+        return
     al = api.Allocator(eng)
     t0 = time.perf_counter()
     w = make_workload(eng, al, args.scale, args.subset)
@@ -608,7 +625,8 @@ def engine_arm(args, ranks):
         wp.free()
         pal.destroy()
         os.rmdir(tmp)
-        ooc["cfg5_subset"] = cfg5_subset(eng, api, W)
+        ooc["cfg5_subset"] = cfg5_subset(eng, api, W, args.cfg5_v_blocks,
+                                         int(args.cfg5_region_gb * 1e9))
 
     configs = None if args.no_configs or ranks.rank != 0 else other_configs(eng, api, W)
 

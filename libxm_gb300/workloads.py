@@ -98,25 +98,41 @@ def symmetric_tensor(lib, alloc, bs, dtype, group, allowed=None):
     return t
 
 
-def fill(t, seed, group=NO_SYM):
+def _block_values(blk, dims, nb, seed, cplx, group):
+    n = int(np.prod(dims))
+    lin = int(np.ravel_multi_index(blk, nb, order="F"))
+    s0 = block_seed(seed, lin)
+    v = uniform(s0, n)
+    if cplx:
+        v = v + 1j * uniform(s0 ^ 0x5555, n)
+    x = v.reshape(dims, order="F")
+    stab = [(p, s) for p, s in group
+            if tuple(blk[p[k]] for k in range(len(blk))) == tuple(blk)]
+    if len(stab) > 1:
+        x = sum(s * np.transpose(x, p) for p, s in stab) / len(stab)
+    return x
+
+
+def fill(t, seed, group=NO_SYM, threads=1):
     """Write seeded uniform[-1,1] data into every canonical block; project
-    blocks that are their own image under the group."""
+    blocks that are their own image under the group.  threads > 1
+    generates the blocks' values on that many threads, a bounded window of
+    blocks at a time (the same values; the writes stay on this thread)."""
     nb = t.nblocks()
     cplx = t.dtype in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX)
-    for blk in t.canonical_blocks():
-        dims = t.block_dims(blk)
-        n = int(np.prod(dims))
-        lin = int(np.ravel_multi_index(blk, nb, order="F"))
-        s0 = block_seed(seed, lin)
-        v = uniform(s0, n)
-        if cplx:
-            v = v + 1j * uniform(s0 ^ 0x5555, n)
-        x = v.reshape(dims, order="F")
-        stab = [(p, s) for p, s in group
-                if tuple(blk[p[k]] for k in range(len(blk))) == tuple(blk)]
-        if len(stab) > 1:
-            x = sum(s * np.transpose(x, p) for p, s in stab) / len(stab)
-        t.write_block(blk, x)
+    blocks = [(blk, t.block_dims(blk)) for blk in t.canonical_blocks()]
+    if threads <= 1:
+        for blk, dims in blocks:
+            t.write_block(blk, _block_values(blk, dims, nb, seed, cplx, group))
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    win = 4 * threads
+    with ThreadPoolExecutor(threads) as ex:
+        for i in range(0, len(blocks), win):
+            part = blocks[i:i + win]
+            vals = ex.map(lambda bd: _block_values(bd[0], bd[1], nb, seed, cplx, group), part)
+            for (blk, _), x in zip(part, vals):
+                t.write_block(blk, x)
 
 
 class Workload:
@@ -144,7 +160,7 @@ class Workload:
 
 
 def ladder(lib, alloc, o_sizes, v_sizes, seed=1, dtype=api.DOUBLE, z2=None,
-           with_c_fill=False, fill_data=True):
+           with_c_fill=False, fill_data=True, threads=1):
     """C(i,j,a,b) = sum_{c,d} A(i,j,c,d) B(c,d,a,b) with i<->j, c<->d, a<->b
     antisymmetry (factor -1 derivative blocks) and optional Z2^3 labels.
     fill_data=False leaves the block data unwritten (for a copy of another
@@ -162,10 +178,10 @@ def ladder(lib, alloc, o_sizes, v_sizes, seed=1, dtype=api.DOUBLE, z2=None,
     c = symmetric_tensor(lib, alloc, sa, dtype, LADDER_ANTISYM, alw_a)
     sa.free(); sb.free()
     if fill_data:
-        fill(a, seed * 3 + 1, LADDER_ANTISYM)
-        fill(b, seed * 3 + 2, LADDER_ANTISYM)
+        fill(a, seed * 3 + 1, LADDER_ANTISYM, threads)
+        fill(b, seed * 3 + 2, LADDER_ANTISYM, threads)
     if with_c_fill and fill_data:
-        fill(c, seed * 3 + 3, LADDER_ANTISYM)
+        fill(c, seed * 3 + 3, LADDER_ANTISYM, threads)
     return Workload("ladder", a, b, c, ("ijcd", "cdab", "ijab"), 1.0, 0.0,
                     (LADDER_ANTISYM, LADDER_ANTISYM, LADDER_ANTISYM),
                     (seed * 3 + 1, seed * 3 + 2, seed * 3 + 3))
@@ -245,7 +261,7 @@ def cfg5_shape(seed=5):
     return o, v, lo, lv
 
 
-def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None):
+def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None, threads=1):
     """Production ladder: o = 128 in 8 blocks of 16, v = 1024 in 32 blocks
     of 24..40, Z2^3 labels.  The full b (vvvv) holds ~275 GB of canonical
     data; v_blocks keeps the first v blocks only (block sizes and labels
@@ -256,7 +272,7 @@ def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None):
         v = [max(1, x // scale) for x in v]
     if v_blocks:
         v, lv = v[:v_blocks], lv[:v_blocks]
-    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv))
+    w = ladder(lib, alloc, o, v, seed, z2=(lo, lv), threads=threads)
     w.name = "cfg5_ladder_o%d_v%d_z2%s" % (sum(o), sum(v), "" if scale == 1 else "_scaled_%d" % scale)
     w.extra = {"o_sizes": o, "v_sizes": v, "o_labels": lo, "v_labels": lv}
     return w

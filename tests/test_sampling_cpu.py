@@ -73,3 +73,16 @@ def test_sampled_gradient_central_differences(oracle):
         x.free()
     w.free()
     al.destroy()
+
+
+def test_threaded_fill_gives_the_same_values(oracle):
+    al = api.Allocator(oracle)
+    w1 = W.cfg2(oracle, al, scale=4)
+    w2 = W.cfg2(oracle, al, scale=4, fill_data=False)
+    W.fill(w2.a, 7, W.LADDER_ANTISYM, threads=4)
+    W.fill(w1.a, 7, W.LADDER_ANTISYM)
+    for blk in w1.a.canonical_blocks():
+        assert np.array_equal(w1.a.read_block(blk), w2.a.read_block(blk))
+    w1.free()
+    w2.free()
+    al.destroy()
