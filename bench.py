@@ -55,12 +55,17 @@ def parse():
     p.add_argument("--scale", type=int, default=1, help="shrink block sizes (debug only)")
     p.add_argument("--subset", type=str, default=None,
                    help="O,V: keep the first O occupied and V virtual blocks (profiling case)")
-    p.add_argument("--cfg5-v-blocks", type=int, default=12,
-                   help="v blocks of the production ladder's structure streamed from a pagefile")
-    p.add_argument("--cfg5-region-gb", type=float, default=2.0,
-                   help="HBM region size for that measurement")
+    p.add_argument("--cfg5-v-blocks", type=int, default=0,
+                   help="v blocks of the production ladder's structure streamed from a "
+                        "pagefile (0: the most, up to 21, that the disk and RAM hold)")
+    p.add_argument("--cfg5-region-gb", type=float, default=32.0,
+                   help="HBM region size for that measurement (32: the engine's default)")
     p.add_argument("--cfg5-only", action="store_true",
                    help="only the production-ladder subset measurement (one JSON line)")
+    p.add_argument("--ring-only", choices=["f32", "c128", "f64"], default=None,
+                   help="only the ring term in that type (profiling case; one JSON line)")
+    p.add_argument("--ring-nv", type=int, default=8,
+                   help="v blocks (of 32) of the ring term for --ring-only")
     return p.parse_args()
 
 
@@ -201,6 +206,24 @@ def cpu_baseline(w, flops, reps=3):
     return res, out
 
 
+def cpu_sample_error(w, chosen, c0, got):
+    """CPU-baseline leg: the CPU reference's result for the chosen canonical
+    output blocks of w's workload (its other output blocks zero, so it
+    does only the sample's work) on the engine's inputs, with the chosen
+    blocks' initial values c0 (beta != 0); relative Frobenius error of the
+    engine's blocks `got` over the sample."""
+    from libxm_gb300 import workloads as W
+    lib, _ = cpu_lib()
+    al = api.Allocator(lib)
+    wc = W.cfg3(lib, al, dtype=w.a.dtype, fill_data=False)
+    W.copy_data(w.a, wc.a)
+    W.copy_data(w.b, wc.b)
+    ref = W.contract_sample(wc, chosen, c0)
+    wc.free()
+    al.destroy()
+    return W.rel_frobenius(got, ref)
+
+
 def block_costs(w):
     """Useful flops per canonical output block (the reference's GEMM work)."""
     import oracle.build as ob
@@ -244,13 +267,15 @@ def timed_calls(eng, fn, reps=3, warm=5):
     return eng.xmg_timer_stop() / reps
 
 
-def other_configs(eng, api, W):
+def other_configs(eng, api, W, check=None):
     """The remaining measured configurations at full size: the plain FP64
     ladder cfg1, the permuted ring term cfg3 in float32 and complex128
     (o = 64 as 4 x 16, v = 256 as 8 x 32, beta = 1, C prefilled), and the
     adjoint of the cfg2 ladder (cfg4: dA and dB in one call).  Accuracy of
     the float32 ring term: against the same contraction in FP64 on the GPU
-    (plain path) over identical, float-rounded inputs."""
+    (plain path) over identical, float-rounded inputs; of the complex128
+    one (when `check`, the CPU-baseline leg's sample check, is given):
+    against the CPU reference on 40 seeded output blocks."""
     out = {}
     al = api.Allocator(eng)
     eng.check(eng.xmg_set_precision(api.PREC_AUTO))
@@ -285,9 +310,19 @@ def other_configs(eng, api, W):
     # cfg3 complex128
     w = W.cfg3(eng, al, dtype=api.DOUBLE_COMPLEX)
     fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(), w.idxc.encode())
+    chosen = W.sample_blocks(w.c.canonical_blocks(), 40, seed=31)
+    c0 = {blk: w.c.read_block(blk) for blk in chosen}
     ms = timed_calls(eng, w.run)
     out["cfg3_ring_o64_v256_c128"] = {"ms": ms, "tflops": fl / ms / 1e9, "useful_flops": fl,
                                       "precision_used": api.last_stats(eng).precision_used}
+    if check is not None:
+        for blk in chosen:                 # beta = 1: restore the sample, one more call
+            w.c.write_block(blk, c0[blk])
+        w.run()
+        got = {blk: w.c.read_block(blk) for blk in chosen}
+        out["cfg3_ring_o64_v256_c128"]["rel_err_vs_oracle_sample"] = check(w, chosen, c0, got)
+        out["cfg3_ring_o64_v256_c128"]["sample"] = "%d of %d canonical output blocks" % (
+            len(chosen), len(w.c.canonical_blocks()))
     w.free()
     # cfg4: the adjoint of the cfg2 ladder, dA and dB
     w = W.cfg2(eng, al)
@@ -369,16 +404,68 @@ def tile_autosplit(eng, api, W, al):
     return res
 
 
-def cfg5_subset(eng, api, W, v_blocks=12, region=int(2e9)):
+def ring_only(eng, api, W, args):
+    """The ring term alone (o = 64 as 4 x 16, v = 32 * ring_nv, beta = 1):
+    `warmup` untimed calls (plan, work-list tuning), then device time per
+    call over `steps` calls and the last call's phases."""
+    dt = {"f32": api.FLOAT, "c128": api.DOUBLE_COMPLEX, "f64": api.DOUBLE}[args.ring_only]
+    al = api.Allocator(eng)
+    w = W.cfg3(eng, al, dtype=dt, nv=args.ring_nv)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(),
+                                w.idxc.encode())
+    ms = timed_calls(eng, w.run, reps=args.steps, warm=args.warmup)
+    st = api.last_stats(eng)
+    out = {"workload": "ring_o64_v%d_%s" % (32 * args.ring_nv, args.ring_only), "ms": ms,
+           "useful_flops": fl, "tflops": fl / ms / 1e9, "gemm_ms": st.ms_gemm,
+           "split_ms": st.ms_split, "policy": st.gemm_policy,
+           "precision_used": st.precision_used}
+    w.free()
+    al.destroy()
+    return out
+
+
+def mem_available():
+    """MemAvailable of /proc/meminfo in bytes (0 if unreadable)."""
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def cfg5_v_blocks_that_fit(W, path, most=21, least=12):
+    """The most v blocks (least..most) whose canonical a, b and c fit the
+    pagefile's file system (10 GB kept free) and half the available RAM
+    (the page cache holds the pagefile while it is streamed)."""
+    import shutil
+    disk = shutil.disk_usage(path).free - 10e9
+    ram = 0.5 * mem_available()
+    for n in range(most, least - 1, -1):
+        if sum(W.cfg5_bytes(n)) <= min(disk, ram):
+            return n, disk, ram
+    return 0, disk, ram
+
+
+def cfg5_subset(eng, api, W, v_blocks=0, region=int(32e9)):
     """The production ladder's structure (o = 128 as 8 x 16, v blocks of
-    24..40 with Z2^3 labels) on its first v_blocks v blocks, all tensors in
-    a pagefile and b streamed through two HBM regions of `region` bytes:
+    24..40 with Z2^3 labels) on its first v_blocks v blocks (0: the most
+    that the host holds, up to 21, where b is 60 GB), all tensors in a
+    pagefile and b streamed through two HBM regions of `region` bytes:
     split-precision against the plain FP64 path on the same inputs, wall
     clock per xm_contract (the first split-precision call plans; the
-    repeated ones reuse the kept streamed plan).  The full b (~275 GB)
-    exceeds the host's disk and RAM."""
+    repeated ones reuse the kept streamed plan).  The full b (~300 GB over
+    32 v blocks) exceeds the host's disk and RAM."""
     import tempfile
     tmp = tempfile.mkdtemp(prefix="xmg_cfg5_")
+    if not v_blocks:
+        v_blocks, disk, ram = cfg5_v_blocks_that_fit(W, tmp)
+        if not v_blocks:
+            os.rmdir(tmp)
+            return {"skipped": "12 v blocks (%.1f GB) exceed the free disk (%.1f GB) or half "
+                               "the available RAM (%.1f GB)"
+                               % (sum(W.cfg5_bytes(12)) / 1e9, disk / 1e9, ram / 1e9)}
     pal = api.Allocator(eng, os.path.join(tmp, "pagefile"))
     t0 = time.perf_counter()
     w = W.cfg5(eng, pal, v_blocks=v_blocks, threads=os.cpu_count() or 1)
@@ -448,6 +535,10 @@ def engine_arm(args, ranks):
     from libxm_gb300 import api, workloads as W
     libxm_gb300.build()
     eng = libxm_gb300.load()
+    if args.ring_only:
+        if ranks.rank == 0:
+            print(json.dumps({"ring_term": ring_only(eng, api, W, args)}))
+        return
     if args.cfg5_only:
         if ranks.rank == 0:
             print(json.dumps({"cfg5_subset": cfg5_subset(
@@ -628,7 +719,8 @@ def engine_arm(args, ranks):
         ooc["cfg5_subset"] = cfg5_subset(eng, api, W, args.cfg5_v_blocks,
                                          int(args.cfg5_region_gb * 1e9))
 
-    configs = None if args.no_configs or ranks.rank != 0 else other_configs(eng, api, W)
+    configs = None if args.no_configs or ranks.rank != 0 else other_configs(
+        eng, api, W, None if args.no_cpu_baseline or ranks.world > 1 else cpu_sample_error)
 
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)

@@ -115,12 +115,13 @@ int xmg_get_last_stats(xmg_stats_t *out);
 
 /* Out-of-core contractions.  When the pagefile blocks of b that a
  * contraction reads exceed `budget` bytes, b is streamed through HBM in
- * batches of at most `region` bytes: two device regions alternate, each
- * batch is read from the pagefile into pinned chunks and copied on a side
- * stream while the previous batch is contracted (c accumulates over the
- * batches; beta is applied once).  a and c are staged whole.  Defaults:
- * 180 GB and 32 GB, or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps
- * the current value. */
+ * about XMG_STAGE_BATCHES (default 8) equal batches of at most `region`
+ * bytes: two device regions alternate, each batch is read from the
+ * pagefile into pinned chunks and copied on a side stream while the
+ * previous batch is contracted (c accumulates over the batches; beta is
+ * applied once).  a and c are staged whole.  Defaults: 180 GB and 32 GB,
+ * or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps the current
+ * value. */
 int xmg_set_staging(size_t budget, size_t region);
 
 /* Hand-written adjoint of c = alpha * a * b over the index strings.  Given
@@ -130,13 +131,30 @@ int xmg_set_staging(size_t budget, size_t region);
  * for L = sum over all blocks of dc o c (the xm_dot pairing), i.e. the
  * contractions dc*b and a*dc projected onto canonical blocks with every
  * derivative block's permutation and scalar folded back.  Either of da, db
- * may be NULL.  Returns XMG_* status. */
+ * may be NULL.  Every canonical block of a (b) must be canonical in da
+ * (db).  When the block tables of a, b and dc are consistent with the
+ * contraction (each derivative block's permutation and scalar carry the
+ * contraction over, checked block by block), each gradient is one
+ * contraction at the canonical positions times a per-block multiplicity;
+ * otherwise it is computed at every nonzero position and folded back
+ * (XMG_ADJOINT_EVERY=1 forces that form).  Returns XMG_* status. */
 int xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
     const xm_tensor_t *b, const xm_tensor_t *dc, xm_tensor_t *da,
     xm_tensor_t *db, const char *idxa, const char *idxb, const char *idxc);
 
-/* For tensors in GPU memory the adjoint keeps its intermediates (W and the
- * gradients at every nonzero position of a and b) and, through the plan
+/* Host-only: the structural checks of xm_contract_adjoint for these
+ * tensors, without a device.  mode[0] (a's gradient) and mode[1] (b's):
+ * 1 = canonical positions with per-block factors, 2 = every nonzero
+ * position.  fa, fb (may be NULL): for the first form, the factor of each
+ * block of a (b) in linear block order (index 0 fastest) as re, im pairs
+ * (2 * number of blocks doubles; zero off the canonical blocks).  Releases
+ * the adjoint's kept intermediates.  Returns XMG_* status. */
+int xmg_adjoint_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
+    const xm_tensor_t *dc, const char *idxa, const char *idxb,
+    const char *idxc, int mode[2], double *fa, double *fb);
+
+/* For tensors in GPU memory the adjoint keeps its intermediates (the
+ * checks' outcome, W and the gradient tensors) and, through the plan
  * cache, the device plans of its two contractions while a, b and dc keep
  * their block structures, so that repeated calls neither plan nor
  * allocate.  This frees them (xmg_plan_cache_clear does too). */
@@ -217,9 +235,11 @@ void xmg_host_free(void *p);
  * read/write calls are plain memory copies.  xm_contract streams the
  * operands of such tensors through HBM on every call: a's blocks (and c's
  * when beta != 0) and b's first batch are copied in, then each further
- * batch of b (about 1/XMG_HOST_BATCHES of it, default 4, at most the
- * staging region) is copied on a side stream while the previous batch is
- * contracted, and c is copied back before the call returns.  The
+ * batch of b is copied on a side stream while the previous batch is
+ * contracted, and c is copied back before the call returns.  The batches
+ * (about XMG_HOST_BATCHES of them, default 8, at most the staging region
+ * each) grow by a factor XMG_HOST_GROWTH (default 1.2) from one to the
+ * next, so that the first copy, which nothing overlaps, is short.  The
  * streamed plan of the last such contraction (batches, HBM regions, the
  * device plans and their graphs) is kept while the tensors' block
  * structures and the call's arguments stay the same (XMG_STREAM_CACHE=0

@@ -132,6 +132,8 @@ _GB_SIGS = {
     "xmg_synchronize": (C.c_int, []),
     "xmg_plan_cache_clear": (None, []),
     "xmg_adjoint_release": (None, []),
+    "xmg_adjoint_plan_check": (C.c_int, [_P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p,
+                                         _P, _P, _P]),
     "xmg_set_staging": (C.c_int, [C.c_size_t, C.c_size_t]),
     "xmg_selftest_bounded_wait": (C.c_int, [C.c_uint]),
     "xmg_block_space_autosplit_tiles": (C.c_int, [_P, C.c_size_t, C.c_size_t]),

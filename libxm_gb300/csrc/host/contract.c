@@ -1510,6 +1510,23 @@ host_first_batch(uint64_t total, double *growth)
 	    (double)total / n;
 }
 
+/* pagefile b beyond the staging budget: about XMG_STAGE_BATCHES (default
+ * 8) equal batches of at most the region's bytes.  The pagefile readers
+ * (page cache, ~40-70 GB/s) are slower than the kernels consume b (about
+ * 100 GB/s for the FP64 ladders), so the call takes about the read time
+ * plus the last batch's kernels: smaller batches shorten that tail.
+ * Returns the batch byte budget. */
+static double
+file_batch(uint64_t total)
+{
+	const char *e = getenv("XMG_STAGE_BATCHES");
+	double n = e ? atof(e) : 8;
+
+	if (n < 1)
+		n = 1;
+	return (double)total / n;
+}
+
 /*
  * The batches, regions and staged views of a streamed contraction (no
  * device plans yet).  Returns XMG_OK with *sp set, or a status; *incore
@@ -1570,6 +1587,8 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		first = host_first_batch(sp->total, &growth);
 	else if (sp->total <= budget)
 		region = sp->total + sp->nu * STAGE_ALIGN;
+	else
+		first = file_batch(sp->total);
 	sp->H = malloc(sp->nu * sizeof *sp->H);
 	sp->SZ = malloc(sp->nu * sizeof *sp->SZ);
 	sp->D = malloc(sp->nu * sizeof *sp->D);

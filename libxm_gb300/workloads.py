@@ -261,6 +261,31 @@ def cfg5_shape(seed=5):
     return o, v, lo, lv
 
 
+def cfg5_bytes(v_blocks=None, seed=5):
+    """Canonical bytes of (a, b, c) of the production ladder on its first
+    v_blocks v blocks, from the shape alone: (anti)symmetric pairs keep
+    one block each (first index <= second), the Z2^3 labels keep the
+    blocks whose four labels xor to 0."""
+    o, v, lo, lv = cfg5_shape(seed)
+    if v_blocks:
+        v, lv = v[:v_blocks], lv[:v_blocks]
+
+    def pairs(sz, lab):
+        # {label: sum of s_p * s_q over canonical pairs p <= q with that label}
+        out = {}
+        for p in range(len(sz)):
+            for q in range(p, len(sz)):
+                k = lab[p] ^ lab[q]
+                out[k] = out.get(k, 0) + sz[p] * sz[q]
+        return out
+
+    po, pv = pairs(o, lo), pairs(v, lv)
+    oo = sum(po[k] * po[k] for k in po)
+    ov = sum(po[k] * pv.get(k, 0) for k in po)
+    vv = sum(pv[k] * pv[k] for k in pv)
+    return 8 * ov, 8 * vv, 8 * ov
+
+
 def cfg5(lib, alloc, seed=5, scale=1, v_blocks=None, threads=1):
     """Production ladder: o = 128 in 8 blocks of 16, v = 1024 in 32 blocks
     of 24..40, Z2^3 labels.  The full b (vvvv) holds ~275 GB of canonical

@@ -120,11 +120,14 @@ def sampled_gradient(lib, al, t, wt, other, idx_w, idx_o, idx_t, alpha, sample, 
         api.contract(alpha, wt, other, 0.0, g, idx_w, idx_o, idx_t)
     else:
         api.contract(alpha, other, wt, 0.0, g, idx_o, idx_w, idx_t)
-    out = {blk: np.zeros(t.block_size(blk)) for blk in sample}
+    cplx = t.dtype in (api.FLOAT_COMPLEX, api.DOUBLE_COMPLEX)
+    out = {blk: np.zeros(t.block_size(blk), dtype=np.complex128 if cplx else np.float64)
+           for blk in sample}
     for blk in positions:
         q = ptr2canon[t.data_ptr(blk)]
         x = g.read_block(blk).reshape(t.block_dims(blk), order="F")
         y = np.transpose(x, np.argsort(t.block_perm(blk)))
-        out[q] += t.block_scalar(blk).real * y.ravel(order="F")
+        s = t.block_scalar(blk)
+        out[q] += (s if cplx else s.real) * y.ravel(order="F")
     g.free()
     return out

@@ -199,3 +199,84 @@ def test_adjoint_kept_intermediates(engine):
             x.free()
         w.free()
         al.destroy()
+
+
+def _adjoint(engine, w, dc, alpha):
+    da, db = w.a.structure(), w.b.structure()
+    api.set_all(da, 0)
+    api.set_all(db, 0)
+    engine.check(engine.xm_contract_adjoint(api.Scalar.of(alpha), w.a.h, w.b.h, dc.h, da.h,
+                                            db.h, w.idxa.encode(), w.idxb.encode(),
+                                            w.idxc.encode()))
+    out = W.read_canonical(da), W.read_canonical(db)
+    da.free()
+    db.free()
+    return out
+
+
+def test_adjoint_forms_agree(engine, monkeypatch):
+    """The ladder's gradients in the symmetric form (canonical positions
+    times multiplicities; the structural checks pass) equal the
+    every-position form forced with XMG_ADJOINT_EVERY=1, in both precision
+    modes."""
+    import test_adjoint_cpu as T
+    al = api.Allocator(engine)
+    w = W.cfg2(engine, al, scale=4)
+    dc = w.c.structure()
+    W.fill(dc, 79, W.LADDER_ANTISYM)
+    assert T.plan_check(engine, w.a, w.b, dc, w.idxa, w.idxb, w.idxc)[0] == [T.SYM, T.SYM]
+    try:
+        for prec in (api.PREC_AUTO, api.PREC_FP64):
+            engine.check(engine.xmg_set_precision(prec))
+            engine.xmg_adjoint_release()
+            sym = _adjoint(engine, w, dc, 1.5)
+            monkeypatch.setenv("XMG_ADJOINT_EVERY", "1")
+            engine.xmg_adjoint_release()
+            every = _adjoint(engine, w, dc, 1.5)
+            monkeypatch.delenv("XMG_ADJOINT_EVERY")
+            for x, y in zip(sym, every):
+                assert W.rel_frobenius(x, y) <= 1e-12, prec
+    finally:
+        engine.check(engine.xmg_set_precision(api.PREC_AUTO))
+        engine.xmg_adjoint_release()
+        dc.free()
+        w.free()
+
+
+@pytest.mark.parametrize("dtype", [api.DOUBLE, api.DOUBLE_COMPLEX])
+def test_adjoint_mixed_forms_vs_oracle(engine, oracle, dtype):
+    """a antisymmetric in the contracted pair (c,d) with b fully canonical:
+    a's gradient falls back to the every-position form, b's takes the
+    symmetric one.  Both against the oracle's exact gradients."""
+    import test_adjoint_cpu as T
+    res = {}
+    for lib in (engine, oracle):
+        al = api.Allocator(lib)
+        o, v = [5, 7], [6, 9, 8]
+        sa = W.make_space(lib, [o, o, v, v])
+        sb = W.make_space(lib, [v, v, v, v])
+        a = W.symmetric_tensor(lib, al, sa, dtype, [((0, 1, 2, 3), 1.0), ((0, 1, 3, 2), -1.0)])
+        b = api.Tensor(lib, sb, dtype, al, canonical=True)
+        c = api.Tensor(lib, sa, dtype, al, canonical=True)
+        W.fill(a, 31, [((0, 1, 2, 3), 1.0), ((0, 1, 3, 2), -1.0)])
+        W.fill(b, 32)
+        dc = c.structure()
+        W.fill(dc, 33)
+        res[lib.path] = (W.Workload("mixed", a, b, c, ("ijcd", "cdab", "ijab"), 1.0, 0.0,
+                                    None, None), dc, al)
+        sa.free()
+        sb.free()
+    (we, dce, _), (wo, dco, oal) = res[engine.path], res[oracle.path]
+    assert T.plan_check(engine, we.a, we.b, dce, we.idxa, we.idxb, we.idxc)[0] == \
+        [T.EVERY, T.SYM]
+    try:
+        gda, gdb = _adjoint(engine, we, dce, -0.5)
+        ea, eb = T.exact_gradients(oracle, oal, wo, dco, -0.5)
+        assert W.rel_frobenius(gda, ea) <= 1e-12
+        assert W.rel_frobenius(gdb, eb) <= 1e-12
+    finally:
+        engine.xmg_adjoint_release()
+        for w, dc, al in res.values():
+            dc.free()
+            w.free()
+            al.destroy()
