@@ -64,6 +64,9 @@ def parse():
                    help="only the production-ladder subset measurement (one JSON line)")
     p.add_argument("--ring-only", choices=["f32", "c128", "f64"], default=None,
                    help="only the ring term in that type (profiling case; one JSON line)")
+    p.add_argument("--ladder-only", action="store_true",
+                   help="only the headline ladder's device time and the adjoint of it "
+                        "(tuning case; one JSON line)")
     p.add_argument("--ring-nv", type=int, default=8,
                    help="v blocks (of 32) of the ring term for --ring-only")
     return p.parse_args()
@@ -424,6 +427,36 @@ def ring_only(eng, api, W, args):
     return out
 
 
+def ladder_only(eng, api, W, args):
+    """The headline ladder (or its --subset / --scale form): device time per
+    xm_contract over `steps` calls after `warmup` untimed ones, the GEMM
+    and split phases of the last call, and the adjoint (dA and dB) of the
+    same ladder, timed the same way."""
+    al = api.Allocator(eng)
+    w = make_workload(eng, al, args.scale, args.subset)
+    fl = eng.xmg_contract_flops(w.a.h, w.b.h, w.c.h, w.idxa.encode(), w.idxb.encode(),
+                                w.idxc.encode())
+    ms = timed_calls(eng, w.run, reps=args.steps, warm=args.warmup)
+    st = api.last_stats(eng)
+    out = {"workload": w.name, "ms": ms, "useful_flops": fl, "tflops": fl / ms / 1e9,
+           "gemm_ms": st.ms_gemm, "split_ms": st.ms_split, "policy": st.gemm_policy}
+    dc = w.c.structure()
+    W.fill(dc, 77, W.LADDER_ANTISYM)
+    da, db = w.a.structure(), w.b.structure()
+
+    def adj():
+        eng.check(eng.xm_contract_adjoint(api.Scalar.of(1.0), w.a.h, w.b.h, dc.h, da.h, db.h,
+                                          b"ijcd", b"cdab", b"ijab"))
+    ams = timed_calls(eng, adj, reps=args.steps, warm=args.warmup)
+    out["adjoint"] = {"ms": ams, "useful_flops": 2 * fl, "tflops": 2 * fl / ams / 1e9}
+    eng.xmg_adjoint_release()
+    for t in (dc, da, db):
+        t.free()
+    w.free()
+    al.destroy()
+    return out
+
+
 def mem_available():
     """MemAvailable of /proc/meminfo in bytes (0 if unreadable)."""
     try:
@@ -535,6 +568,10 @@ def engine_arm(args, ranks):
     from libxm_gb300 import api, workloads as W
     libxm_gb300.build()
     eng = libxm_gb300.load()
+    if args.ladder_only:
+        if ranks.rank == 0:
+            print(json.dumps({"ladder": ladder_only(eng, api, W, args)}))
+        return
     if args.ring_only:
         if ranks.rank == 0:
             print(json.dumps({"ring_term": ring_only(eng, api, W, args)}))

@@ -441,7 +441,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ EA,
     const int32_t *__restrict__ EB, const int32_t *__restrict__ cbF,
-    double alpha, double beta, int expoff2, int cplx, int hmax,
+    double alpha, double beta, int expoff2, int cplx, int hmax, int pfd,
     int *__restrict__ flags)
 {
 	using C = stage_cfg<S>;
@@ -587,51 +587,96 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				}
 				/* shared side from a's views when it is a's side */
 				const bool sha = (mstk ^ swp) != 0;
-				for (int p = 0; p < cb.npairs && !s_err; p++) {
-					/* the members' pair lists run in step: pair p of every
-					 * member has member 0's view and K on the shared side */
+				/* a pair's operand chunks: the shared side's tile (live
+				 * or past the view) and each member's */
+				struct pair_src {
+					const uint8_t *gs, *gn[EMU_MAXMEM];
+					int nks;
+					bool slive;
+				};
+				auto load_pair = [&](int p, pair_src &o) {
+					/* the members' pair lists run in step: pair p of
+					 * every member has member 0's view and K on the
+					 * shared side */
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
 					const xmgd_view_t ws = sha ? va[pr.aview] : vb[pr.bview];
-					const int nks = vb[pr.bview].n_ks, nh = nks / 2;
+					o.nks = vb[pr.bview].n_ks;
 					const int stile = it.m0 / EMU_TM + (mstk ? 0 : (int)rank);
-					const bool slive = stile < ws.n_rt;
-					const uint8_t *gs = reinterpret_cast<const uint8_t *>(ws.slices) +
-					    (size_t)stile * nks * C::CHUNK_BYTES;
-					const uint8_t *gn[EMU_MAXMEM];
+					o.slive = stile < ws.n_rt;
+					o.gs = reinterpret_cast<const uint8_t *>(ws.slices) +
+					    (size_t)stile * o.nks * C::CHUNK_BYTES;
 #pragma unroll
 					for (int j = 0; j < EMU_MAXMEM; j++) {
 						const xmgd_pair_t pj = prs[mfp[j] + p];
-						gn[j] = reinterpret_cast<const uint8_t *>(sha ?
+						o.gn[j] = reinterpret_cast<const uint8_t *>(sha ?
 						    vb[pj.bview].slices : va[pj.aview].slices) +
-						    (size_t)mrt[j] * nks * C::CHUNK_BYTES + noff;
+						    (size_t)mrt[j] * o.nks * C::CHUNK_BYTES + noff;
 					}
-					for (int ks = 0; ks < nks; ks++) {
+				};
+				/* K step ks of a pair: the shared side reads at its own
+				 * K index (the M side's or the N side's), the members at
+				 * the other; the imaginary pass swaps B's re/im halves */
+				auto kidx = [&](int ks, int nks, int &ksh, int &kst) {
+					const int nh = nks / 2;
+					const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
+					const int km = swp ? ks : kb, kn = swp ? kb : ks;
+					ksh = mstk ? kn : km;
+					kst = mstk ? km : kn;
+				};
+				/* L2 prefetch cursor, pfd steps ahead of the copies within
+				 * the item (XMG_EMU_PF; off by default: measured slower,
+				 * the ring's copies are not waiting on DRAM misses) */
+				pair_src pf;
+				int pfp = 0, pfk = 0;
+				if (pfd > 0)
+					load_pair(0, pf);
+				auto pf_step = [&]() {
+					if (pfd <= 0 || pfp >= cb.npairs)
+						return;
+					int ksh, kst;
+					kidx(pfk, pf.nks, ksh, kst);
+					if (pf.slive)
+						bulk_prefetch_l2(pf.gs + (size_t)ksh * C::CHUNK_BYTES, shb);
+#pragma unroll
+					for (int j = 0; j < EMU_MAXMEM; j++)
+						if (j < nmem)
+							bulk_prefetch_l2(pf.gn[j] + (size_t)kst * C::CHUNK_BYTES,
+							    mby[j]);
+					if (++pfk == pf.nks) {
+						pfk = 0;
+						if (++pfp < cb.npairs)
+							load_pair(pfp, pf);
+					}
+				};
+				for (int q = 0; q < pfd; q++)
+					pf_step();
+				pair_src cur;
+				for (int p = 0; p < cb.npairs && !s_err; p++) {
+					load_pair(p, cur);
+					for (int ks = 0; ks < cur.nks; ks++) {
 						if (!wait(smem_u32(&bar_empty[s]), ph ^ 1, 1))
 							break;
-						/* imaginary pass: B's re/im halves swapped */
-						const int kb = (cplx && pass) ? (ks < nh ? ks + nh : ks - nh) : ks;
-						const int km = swp ? ks : kb, kn = swp ? kb : ks;
 						uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 						uint32_t fb = smem_u32(&bar_full[s]);
-						/* the shared side reads at its own K index (the
-						 * M side's or the N side's), the members at the
-						 * other; a pair's second M tile may lie past the
-						 * view: its rows are then never stored */
-						const int ksh = mstk ? kn : km, kst = mstk ? km : kn;
-						mbar_expect_tx(fb, (slive ? shb : 0) + stb);
-						if (slive)
+						/* a pair's second M tile may lie past the view: its
+						 * rows are then never stored */
+						int ksh, kst;
+						kidx(ks, cur.nks, ksh, kst);
+						mbar_expect_tx(fb, (cur.slive ? shb : 0) + stb);
+						if (cur.slive)
 							bulk_g2s(dst + (mstk ? C::CHUNK_BYTES : 0u),
-							    gs + (size_t)ksh * C::CHUNK_BYTES, shb, fb);
+							    cur.gs + (size_t)ksh * C::CHUNK_BYTES, shb, fb);
 #pragma unroll
 						for (int j = 0; j < EMU_MAXMEM; j++)
 							if (j < nmem)
 								bulk_g2s(dst + mdo[j],
-								    gn[j] + (size_t)kst * C::CHUNK_BYTES, mby[j], fb);
+								    cur.gn[j] + (size_t)kst * C::CHUNK_BYTES, mby[j], fb);
 #pragma unroll
 						for (int q = 0; q < NST; q++)
 							if (q == s)
 								lastp[q] = (int)ph;
 						if (++s == NST) { s = 0; ph ^= 1; }
+						pf_step();
 					}
 				}
 			}
@@ -1161,6 +1206,7 @@ struct emu_plan {
 	std::vector<emu_cand> cand;
 	int cur = 0, tuned = 0;
 	int hmax = 4;                        /* head/tail steps (<= stages) */
+	int pfd = 0;                         /* L2 prefetch distance, steps */
 	uint64_t sig = 0;
 	int *h_flags = nullptr;              /* pinned: Inf/NaN, timeout */
 	int (*split)(emu_plan *) = nullptr;
@@ -1232,7 +1278,7 @@ launch_gemm(emu_plan *e)
 		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    (const int32_t *)EA, (const int32_t *)EB, (const int32_t *)e->d_F,
-		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags));
+		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, flags));
 	} else {
 		emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, false><<<(unsigned)c.grid,
 		    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
@@ -1240,7 +1286,7 @@ launch_gemm(emu_plan *e)
 		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
-		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, flags);
+		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, flags);
 	}
 	g_launches++;
 	XMG_CK(cudaGetLastError());
@@ -1617,6 +1663,8 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		const char *h = getenv("XMG_EMU_HEAD");
 		e->hmax = h ? atoi(h) : 4;
 		e->hmax = std::max(1, std::min(nst, e->hmax));
+		const char *f = getenv("XMG_EMU_PF");
+		e->pfd = f ? std::max(0, atoi(f)) : 0;
 	}
 	e->alpha = p->alpha[0];
 	e->beta = p->beta[0];

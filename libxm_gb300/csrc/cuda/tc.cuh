@@ -108,6 +108,14 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src,
 	    : "memory");
 }
 
+/* bring [src, src + bytes) into L2 ahead of its shared-memory copy
+ * (address and size multiples of 16 bytes) */
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
+{
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;"
+	    :: "l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before()
 {
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -420,7 +420,9 @@ struct adj_side {
 };
 
 static struct {
-	const xm_tensor_t *a, *b, *dc;
+	const xm_tensor_t *a, *b, *dc;	/* identity only: never dereferenced,
+					   they may have been freed since */
+	const xm_allocator_t *al_a, *al_b;	/* where the kept tensors live */
 	uint64_t ga_gen, gb_gen, gdc_gen;
 	char idx[3][XM_MAX_DIM + 1];
 	int fwd;		/* forward check: -1 not run, 0 failed, 1 passed */
@@ -447,7 +449,7 @@ xmg_adjoint_release(void)
 void
 xmg_adjoint_forget(const xm_allocator_t *al)
 {
-	if (g_adj.a != NULL && g_adj.a->allocator == al)
+	if (al != NULL && (g_adj.al_a == al || g_adj.al_b == al))
 		xmg_adjoint_release();
 }
 
@@ -536,6 +538,8 @@ xm_contract_adjoint(xm_scalar_t alpha, const xm_tensor_t *a,
 	    xmg_alloc_is_device(a->allocator))) {
 		xmg_adjoint_release();
 		g_adj.a = a; g_adj.b = b; g_adj.dc = dc;
+		g_adj.al_a = a->allocator;
+		g_adj.al_b = b->allocator;
 		g_adj.ga_gen = a->gen; g_adj.gb_gen = b->gen;
 		g_adj.gdc_gen = dc->gen;
 		strcpy(g_adj.idx[0], idxa);
