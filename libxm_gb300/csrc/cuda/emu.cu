@@ -35,8 +35,8 @@
  *     warp 0 streams stages with cp.async.bulk, warp 1 issues the slice
  *     products per 16-wide K step with tcgen05.mma.kind::f16 (bf16 x bf16 ->
  *     fp32) into TMEM accumulators, warps 2..17 drain them every 160 K
- *     elements for FP64 and every <= 336 for FP32 (the exact groups stay
- *     below 3 * 336 * 2^14 < 2^24, exact in fp32) into
+ *     elements for FP64 and every <= 320 for FP32 (the exact groups stay
+ *     below 3 * 320 * 2^14 < 2^24, exact in fp32) into
  *     per-thread int64 fixed-point sums in units of 2^(-16-F), applying the
  *     pair factor exactly.  The epilogue is the only FP64 work:
  *     C = alpha * 2^(eA + eB - 2 * EXPOFF - 16 - F) * V + beta * C, scattered
@@ -60,7 +60,7 @@ namespace xmg {
 constexpr int EMU_TM = 128;              /* rows per tile, both operands */
 constexpr int EMU_KS = 16;               /* K per stage = K per MMA */
 constexpr int EMU_CHUNK = 10;            /* K steps per chunk, FP64 (160) */
-constexpr int EMU_CHUNK32 = 21;          /* K steps per chunk at most, FP32 */
+constexpr int EMU_CHUNK32 = 20;          /* K steps per chunk at most, FP32 */
 constexpr int SLICE_BYTES = EMU_TM * EMU_KS * 2;          /* 4096 */
 #ifndef EMU_DW
 #define EMU_DW 16                        /* drain warps: 8 or 16 */
@@ -360,30 +360,69 @@ __device__ __forceinline__ bool pack_f64(long long V, int e, unsigned long long 
 	return true;
 }
 
+/* A pipeline stage holds KSTEPS consecutive 16-wide K steps (each the
+ * M-side chunk then the N-side chunk).  The 3-slice form issues only 6
+ * MMAs per K step, so it takes two steps per stage: the per-stage
+ * synchronisation of the producer and MMA threads (barrier round trips,
+ * copy issue, commit) would otherwise take longer than the step's MMAs
+ * (measured: removing every copy, or every MMA, left the float32 GEMM
+ * within 6 % of its time at one step per stage). */
 template <int S>
 struct stage_cfg {
+	static constexpr int KSTEPS = S == fin<float>::S ? 2 : 1;
 	static constexpr int CHUNK_BYTES = S * SLICE_BYTES;
-	static constexpr int STAGE_BYTES = 2 * CHUNK_BYTES;
+	static constexpr int STEP_BYTES = 2 * CHUNK_BYTES;
+	static constexpr int STAGE_BYTES = KSTEPS * STEP_BYTES;
 	static constexpr int NST = STAGE_BUDGET / STAGE_BYTES > 8 ? 8 :
 	    STAGE_BUDGET / STAGE_BYTES;
 	static constexpr int SMEM = NST * STAGE_BYTES + 1024;
 };
+
+/* the end of the K segment holding step k: the pair, or the re/im half
+ * of a realified complex view */
+__device__ __forceinline__ int segment_end(int k, int nks, int cplx)
+{
+	return (cplx && k < nks / 2) ? nks / 2 : nks;
+}
+
+/* the stage that starts at step k holds steps [k, super_end): KSTEPS of
+ * them, never past the segment's end */
+template <int S>
+__device__ __forceinline__ int super_end(int k, int nks, int cplx)
+{
+	return min(segment_end(k, nks, cplx), k + stage_cfg<S>::KSTEPS);
+}
+
+/* stages per pair: each segment in stages of KSTEPS steps */
+template <int S>
+__device__ __forceinline__ int stages_of(int nks, int cplx)
+{
+	constexpr int KS = stage_cfg<S>::KSTEPS;
+	if (!cplx)
+		return (nks + KS - 1) / KS;
+	const int nh = nks / 2;
+	return (nh + KS - 1) / KS + (nks - nh + KS - 1) / KS;
+}
 
 /* K steps [c0, c1) of the next chunk: chunks never straddle the re/im
  * boundary of a realified complex view.  An exact group g accumulates at
  * most 3 products of |d_p d_q| <= 2^14 per K element, so its integer sum
  * stays below 2^24 (exact in fp32) for chunks of up to 341 elements.
  * FP64 keeps 160 (its rounded low band's error grows with the chunk);
- * FP32, all exact, takes up to 21 steps (336), the steps left split into
- * equal chunks (32 steps: 16 + 16, not 21 + 11). */
+ * FP32, all exact, takes up to 20 steps (320), the steps left split into
+ * equal chunks of whole stages (32 steps: 16 + 16, not 20 + 12), so that
+ * the stages of a segment, which start at its first step, never straddle
+ * a chunk boundary. */
 template <int S>
 __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 {
-	const int lim = (cplx && c0 < nks / 2) ? nks / 2 : nks;
+	const int lim = segment_end(c0, nks, cplx);
 	if constexpr (S == fin<float>::S) {
+		constexpr int KS = stage_cfg<S>::KSTEPS;
 		const int left = lim - c0;
 		const int n = (left + EMU_CHUNK32 - 1) / EMU_CHUNK32;
-		return c0 + (left + n - 1) / n;
+		const int len = ((left + n - 1) / n + KS - 1) / KS * KS;
+		return min(lim, c0 + len);
 	}
 	return min(lim, c0 + EMU_CHUNK);
 }
@@ -653,30 +692,36 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 				pair_src cur;
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
 					load_pair(p, cur);
-					for (int ks = 0; ks < cur.nks; ks++) {
+					for (int ks = 0; ks < cur.nks; ) {
 						if (!wait(smem_u32(&bar_empty[s]), ph ^ 1, 1))
 							break;
+						const int ke = super_end<S>(ks, cur.nks, cplx);
 						uint32_t dst = smem_u32(stages + (size_t)s * C::STAGE_BYTES);
 						uint32_t fb = smem_u32(&bar_full[s]);
 						/* a pair's second M tile may lie past the view: its
 						 * rows are then never stored */
-						int ksh, kst;
-						kidx(ks, cur.nks, ksh, kst);
-						mbar_expect_tx(fb, (cur.slive ? shb : 0) + stb);
-						if (cur.slive)
-							bulk_g2s(dst + (mstk ? C::CHUNK_BYTES : 0u),
-							    cur.gs + (size_t)ksh * C::CHUNK_BYTES, shb, fb);
+						mbar_expect_tx(fb, (uint32_t)(ke - ks) *
+						    ((cur.slive ? shb : 0) + stb));
+						for (int k = ks; k < ke; k++, dst += C::STEP_BYTES) {
+							int ksh, kst;
+							kidx(k, cur.nks, ksh, kst);
+							if (cur.slive)
+								bulk_g2s(dst + (mstk ? C::CHUNK_BYTES : 0u),
+								    cur.gs + (size_t)ksh * C::CHUNK_BYTES, shb, fb);
 #pragma unroll
-						for (int j = 0; j < EMU_MAXMEM; j++)
-							if (j < nmem)
-								bulk_g2s(dst + mdo[j],
-								    cur.gn[j] + (size_t)kst * C::CHUNK_BYTES, mby[j], fb);
+							for (int j = 0; j < EMU_MAXMEM; j++)
+								if (j < nmem)
+									bulk_g2s(dst + mdo[j],
+									    cur.gn[j] + (size_t)kst * C::CHUNK_BYTES,
+									    mby[j], fb);
+							pf_step();
+						}
 #pragma unroll
 						for (int q = 0; q < NST; q++)
 							if (q == s)
 								lastp[q] = (int)ph;
 						if (++s == NST) { s = 0; ph ^= 1; }
-						pf_step();
+						ks = ke;
 					}
 				}
 			}
@@ -708,8 +753,8 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					break;
 				const xmgd_cblock_t cb = cbs[members[items[t].mfirst].cblock];
 				for (int p = 0; p < cb.npairs && !s_err; p++) {
-					const int nks = vb[prs[cb.first_pair + p].bview].n_ks;
-					for (int ks = 0; ks < nks; ks++) {
+					const int nst_p = stages_of<S>(vb[prs[cb.first_pair + p].bview].n_ks, cplx);
+					for (int q = 0; q < nst_p; q++) {
 						if (!wait(smem_u32(&bar_full[s]), ph, 3))
 							break;
 						mbar_arrive_remote(map_shared(smem_u32(&bar_pfull[s]), 0));
@@ -755,13 +800,10 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					const int nks = vb[pr.bview].n_ks;
 					for (int c0 = 0; c0 < nks && !s_err; ) {
 						const int c1 = chunk_end<S>(c0, nks, cplx);
-						/* head: the first H (staged) steps; tail: the last T
-						 * steps; middle: the rest.  H, T <= hmax <= NST: the
-						 * stages a head or tail holds are released only after
-						 * its set-Y products, so hmax < NST leaves stages for
-						 * the producer to prefetch the steps after them */
-						const int H = min(hmax, c1 - c0);
-						const int T = min(hmax, c1 - c0 - H);
+						/* the chunk's stages: KSTEPS steps each, the last
+						 * one shorter at a segment's end */
+						constexpr int KS = C::KSTEPS;
+						const int nss = (c1 - c0 + KS - 1) / KS;
 						/* every accumulator restarts each chunk: the exact
 						 * groups for their 2^24 bound, the low band because
 						 * the tensor core's fp32 accumulation error grows
@@ -769,6 +811,20 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						 * accumulation measured 10x larger error) */
 						uint32_t started = 0;
 						bool okc = true;
+						auto issue_stage = [&](int sj, int j, int which) {
+							const uint32_t base = smem_u32(stages + (size_t)sj * C::STAGE_BYTES);
+							const int nk = min(KS, c1 - c0 - j * KS);
+							for (int u = 0; u < nk; u++)
+								issue_step<S, KEEP, PAIR>(tmem, base + u * C::STEP_BYTES,
+								    C::CHUNK_BYTES, idesc, which, started);
+						};
+						/* head: the first H (staged) stages; tail: the last T
+						 * stages; middle: the rest.  H, T <= hmax <= NST: the
+						 * stages a head or tail holds are released only after
+						 * its set-Y products, so hmax < NST leaves stages for
+						 * the producer to prefetch the steps after them */
+						const int H = min(hmax, nss);
+						const int T = min(hmax, nss - H);
 						/* head, set X, as soon as the drain has read X of
 						 * the previous chunk */
 						if (!first) {
@@ -785,8 +841,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
-							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
+							issue_stage(sj, j, 1);
 						}
 						if (!okc)
 							break;
@@ -802,27 +857,25 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 						tc_fence_after();
 						for (int j = 0; j < H; j++) {
 							const int sj = s + j < NST ? s + j : s + j - NST;
-							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
-							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
+							issue_stage(sj, j, 2);
 							commit(&bar_empty[sj]);
 						}
 						s += H;
 						if (s >= NST) { s -= NST; ph ^= 1; }
-						/* middle: every product per step */
-						for (int ks = c0 + H; ks < c1 - T; ks++) {
+						/* middle: every product per stage */
+						for (int j = H; j < nss - T; j++) {
 							if (!ready(s, ph)) {
 								okc = false;
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)s *
-							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 3, started);
+							issue_stage(s, j, 3);
 							commit(&bar_empty[s]);
 							if (++s == NST) { s = 0; ph ^= 1; }
 						}
 						if (!okc)
 							break;
-						/* tail: set X of the last T steps, then X is
+						/* tail: set X of the last T stages, then X is
 						 * complete and its drain can start while the
 						 * tensor core still works on set Y */
 						for (int j = 0; j < T; j++) {
@@ -833,8 +886,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 								break;
 							}
 							tc_fence_after();
-							issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
-							    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 1, started);
+							issue_stage(sj, nss - T + j, 1);
 						}
 						if (!okc)
 							break;
@@ -842,8 +894,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 							commit(&bar_xfull);
 							for (int j = 0; j < T; j++) {
 								const int sj = s + j < NST ? s + j : s + j - NST;
-								issue_step<S, KEEP, PAIR>(tmem, smem_u32(stages + (size_t)sj *
-								    C::STAGE_BYTES), C::CHUNK_BYTES, idesc, 2, started);
+								issue_stage(sj, nss - T + j, 2);
 								commit(&bar_empty[sj]);
 							}
 							s += T;
@@ -1024,7 +1075,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 #pragma unroll
 						for (int c = 0; c < 4; c++) {
 							/* exact integers: with the pair factor's 2^1,
-							 * |i0| <= 2^14 * 336 * 2 < 2^23.4 and |i1| <
+							 * |i0| <= 2^14 * 320 * 2 < 2^23.4 and |i1| <
 							 * 2^24.4; the packing is 64-bit */
 							int i0 = __float2int_rn(a0[c] * sa);
 							int i1 = __float2int_rn(a1[c] * sb);
@@ -1660,8 +1711,10 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	e->cplx = cplx;
 	{
 		const int nst = dbl ? stage_cfg<fin<double>::S>::NST : stage_cfg<fin<float>::S>::NST;
+		/* head/tail length in stages: 4 one-step stages (FP64), 2
+		 * two-step stages (FP32) */
 		const char *h = getenv("XMG_EMU_HEAD");
-		e->hmax = h ? atoi(h) : 4;
+		e->hmax = h ? atoi(h) : (dbl ? 4 : 2);
 		e->hmax = std::max(1, std::min(nst, e->hmax));
 		const char *f = getenv("XMG_EMU_PF");
 		e->pfd = f ? std::max(0, atoi(f)) : 0;
