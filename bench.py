@@ -270,6 +270,16 @@ def timed_calls(eng, fn, reps=3, warm=5):
     return eng.xmg_timer_stop() / reps
 
 
+def adjoint_modes(eng, api, w, dc):
+    """The form xm_contract_adjoint takes for each gradient (1 symmetric,
+    2 every position), from its host-only checks."""
+    import ctypes
+    mode = (ctypes.c_int * 2)()
+    eng.check(eng.xmg_adjoint_plan_check(w.a.h, w.b.h, dc.h, w.idxa.encode(), w.idxb.encode(),
+                                         w.idxc.encode(), mode, None, None))
+    return list(mode)
+
+
 def other_configs(eng, api, W, check=None):
     """The remaining measured configurations at full size: the plain FP64
     ladder cfg1, the permuted ring term cfg3 in float32 and complex128
@@ -360,9 +370,10 @@ def other_configs(eng, api, W, check=None):
         "fp64_plain": {"ms": ms64, "tflops": 2 * fl / ms64 / 1e9},
         "speedup_vs_fp64_plain": ms64 / ms,
         "rel_err_vs_fp64": W.rel_frobenius(g_emu, g_64),
-        "note": "dA and dB in one call: the gradient contractions at every nonzero "
-                "position of A and B (about 4x the useful flops of the forward "
-                "pair), then the folds onto canonical blocks"}
+        "form": "symmetric" if adjoint_modes(eng, api, w, dc) == [1, 1] else "every position",
+        "note": "dA and dB in one call; symmetric form: each gradient one contraction "
+                "at the canonical positions of A (B), then a per-block multiplicity "
+                "scale (the structural checks pass for the antisymmetric ladder)"}
     for x in (dc, da, db):
         x.free()
     w.free()

@@ -34,7 +34,7 @@
  *  3. emu_gemm_kernel  - one CTA per (output block, 128 x 128 tile, pass);
  *     warp 0 streams stages with cp.async.bulk, warp 1 issues the slice
  *     products per 16-wide K step with tcgen05.mma.kind::f16 (bf16 x bf16 ->
- *     fp32) into TMEM accumulators, warps 2..17 drain them every 160 K
+ *     fp32) into TMEM accumulators, warps 2..17 drain them every 256 K
  *     elements for FP64 and every <= 320 for FP32 (the exact groups stay
  *     below 3 * 320 * 2^14 < 2^24, exact in fp32) into
  *     per-thread int64 fixed-point sums in units of 2^(-16-F), applying the
@@ -59,7 +59,7 @@ namespace xmg {
 
 constexpr int EMU_TM = 128;              /* rows per tile, both operands */
 constexpr int EMU_KS = 16;               /* K per stage = K per MMA */
-constexpr int EMU_CHUNK = 10;            /* K steps per chunk, FP64 (160) */
+constexpr int EMU_CHUNK = 16;            /* K steps per chunk, FP64 (256) */
 constexpr int EMU_CHUNK32 = 20;          /* K steps per chunk at most, FP32 */
 constexpr int SLICE_BYTES = EMU_TM * EMU_KS * 2;          /* 4096 */
 #ifndef EMU_DW
@@ -408,13 +408,15 @@ __device__ __forceinline__ int stages_of(int nks, int cplx)
  * boundary of a realified complex view.  An exact group g accumulates at
  * most 3 products of |d_p d_q| <= 2^14 per K element, so its integer sum
  * stays below 2^24 (exact in fp32) for chunks of up to 341 elements.
- * FP64 keeps 160 (its rounded low band's error grows with the chunk);
+ * FP64 takes 256 (XMG_EMU_CHUNK steps, at most 20): its rounded low
+ * band's error grows with the chunk (cfg2 ladder: 3.1e-13 at 160, 4.4e-13
+ * at 224, 6.2e-13 at 320, against GEMM times of 35.8, 34.2 and 33.2 ms);
  * FP32, all exact, takes up to 20 steps (320), the steps left split into
  * equal chunks of whole stages (32 steps: 16 + 16, not 20 + 12), so that
  * the stages of a segment, which start at its first step, never straddle
  * a chunk boundary. */
 template <int S>
-__device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
+__device__ __forceinline__ int chunk_end(int c0, int nks, int cplx, int kchunk)
 {
 	const int lim = segment_end(c0, nks, cplx);
 	if constexpr (S == fin<float>::S) {
@@ -424,7 +426,7 @@ __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx)
 		const int len = ((left + n - 1) / n + KS - 1) / KS * KS;
 		return min(lim, c0 + len);
 	}
-	return min(lim, c0 + EMU_CHUNK);
+	return min(lim, c0 + kchunk);
 }
 
 /* Accumulators: 0, 1, 2 hold the exact weight groups p + q = 0, 1, 2; 3
@@ -480,7 +482,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
     const xmgd_view_t *__restrict__ va, const xmgd_view_t *__restrict__ vb,
     const int32_t *__restrict__ tabs, const int32_t *__restrict__ EA,
     const int32_t *__restrict__ EB, const int32_t *__restrict__ cbF,
-    double alpha, double beta, int expoff2, int cplx, int hmax, int pfd,
+    double alpha, double beta, int expoff2, int cplx, int hmax, int pfd, int kchunk,
     int *__restrict__ flags)
 {
 	using C = stage_cfg<S>;
@@ -799,7 +801,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					const xmgd_pair_t pr = prs[cb.first_pair + p];
 					const int nks = vb[pr.bview].n_ks;
 					for (int c0 = 0; c0 < nks && !s_err; ) {
-						const int c1 = chunk_end<S>(c0, nks, cplx);
+						const int c1 = chunk_end<S>(c0, nks, cplx, kchunk);
 						/* the chunk's stages: KSTEPS steps each, the last
 						 * one shorter at a segment's end */
 						constexpr int KS = C::KSTEPS;
@@ -992,7 +994,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 					esh[g] = pg.eshift;
 				}
 				for (int c0 = 0; c0 < nks; ) {
-					const int c1 = chunk_end<S>(c0, nks, cplx);
+					const int c1 = chunk_end<S>(c0, nks, cplx, kchunk);
 					/* each segment's pair factor sign * 2^shift (shift 0
 					 * or 1, checked by the planner) rides on the exact
 					 * fp32 -> int scales; the real pass negates the im * im
@@ -1258,6 +1260,7 @@ struct emu_plan {
 	int cur = 0, tuned = 0;
 	int hmax = 4;                        /* head/tail steps (<= stages) */
 	int pfd = 0;                         /* L2 prefetch distance, steps */
+	int kchunk = EMU_CHUNK;              /* FP64: K steps per chunk */
 	uint64_t sig = 0;
 	int *h_flags = nullptr;              /* pinned: Inf/NaN, timeout */
 	int (*split)(emu_plan *) = nullptr;
@@ -1329,7 +1332,7 @@ launch_gemm(emu_plan *e)
 		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    (const int32_t *)EA, (const int32_t *)EB, (const int32_t *)e->d_F,
-		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, flags));
+		    e->alpha, e->beta, 2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, e->kchunk, flags));
 	} else {
 		emu_gemm_kernel<S, KEEP, LOW, TOUT, EMU_DW, false><<<(unsigned)c.grid,
 		    64 + 32 * EMU_DW, stage_cfg<S>::SMEM, stream()>>>(
@@ -1337,7 +1340,7 @@ launch_gemm(emu_plan *e)
 		    e->d_cbs, e->d_prs,
 		    (const xmgd_view_t *)e->d_va, (const xmgd_view_t *)e->d_vb, e->d_tabs,
 		    EA, EB, (const int32_t *)e->d_F, e->alpha, e->beta,
-		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, flags);
+		    2 * fin<TIN>::EXPOFF, e->cplx, e->hmax, e->pfd, e->kchunk, flags);
 	}
 	g_launches++;
 	XMG_CK(cudaGetLastError());
@@ -1716,6 +1719,8 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 		const char *h = getenv("XMG_EMU_HEAD");
 		e->hmax = h ? atoi(h) : (dbl ? 4 : 2);
 		e->hmax = std::max(1, std::min(nst, e->hmax));
+		const char *kc = getenv("XMG_EMU_CHUNK");
+		e->kchunk = kc ? std::max(1, std::min(20, atoi(kc))) : EMU_CHUNK;
 		const char *f = getenv("XMG_EMU_PF");
 		e->pfd = f ? std::max(0, atoi(f)) : 0;
 	}
