@@ -116,10 +116,13 @@ int xmg_get_last_stats(xmg_stats_t *out);
 /* Out-of-core contractions.  When the pagefile blocks of b that a
  * contraction reads exceed `budget` bytes, b is streamed through HBM in
  * about XMG_STAGE_BATCHES (default 8) equal batches of at most `region`
- * bytes: two device regions alternate, each batch is read from the
- * pagefile into pinned chunks and copied on a side stream while the
- * previous batch is contracted (c accumulates over the batches; beta is
- * applied once).  a and c are staged whole.  Defaults: 180 GB and 32 GB,
+ * bytes: two device regions alternate, each batch is copied on a side
+ * stream while the previous batch is contracted (c accumulates over the
+ * batches; beta is applied once).  Where the device reads pageable host
+ * memory through the host's page tables (a coherent CPU-GPU link) the
+ * copies read the pagefile's blocks straight from a read-only mapping of
+ * the file, else reader threads read them into pinned chunks first
+ * (XMG_STAGE_MMAP=0 / 1 forces either).  a and c are staged whole.  Defaults: 180 GB and 32 GB,
  * or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps the current
  * value. */
 int xmg_set_staging(size_t budget, size_t region);

@@ -219,6 +219,22 @@ xmgd_pinned(size_t bytes, void **hptr)
 	return XMG_OK;
 }
 
+/* 1 when the engine's device reads pageable host memory through the
+ * host's page tables (a coherent CPU-GPU link, e.g. Grace): copies from
+ * any host mapping then run at the link's rate without staging */
+extern "C" int
+xmgd_pageable_direct(void)
+{
+	int v = 0;
+
+	if (cudaDeviceGetAttribute(&v,
+	    cudaDevAttrPageableMemoryAccessUsesHostPageTables, g_dev) != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	return v;
+}
+
 /* make the calling host thread use the engine's device */
 extern "C" int
 xmgd_bind_thread(void)

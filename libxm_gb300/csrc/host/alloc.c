@@ -23,6 +23,8 @@
 #include <fcntl.h>
 #include <unistd.h>
 
+#include <sys/mman.h>
+
 #include "xmg_host.h"
 #include "hmap.h"
 
@@ -40,6 +42,8 @@ struct xm_allocator {
 	xmg_hmap_t views;         /* pagefile: handle -> staged device addr */
 	xmg_hmap_t bviews;        /* pagefile: handle -> view inside `bulk` */
 	uint64_t bulk;            /* one HBM buffer holding the bulk views */
+	const unsigned char *map; /* pagefile: read-only mapping of the file */
+	uint64_t map_bytes;       /* its length (the file's when mapped) */
 };
 
 static int bit_get(const unsigned char *b, uint64_t i) { return (b[i >> 3] >> (i & 7)) & 1; }
@@ -414,6 +418,52 @@ xmg_alloc_view_addr(const xm_allocator_t *a, uint64_t h)
 	return 0;
 }
 
+/*
+ * A read-only shared mapping of the pagefile up to its last used page, for
+ * streaming its blocks to the device with the copy engine straight from
+ * the page cache (where the device reads pageable memory through the
+ * host's page tables; the file's own writes, pwrite, are visible through
+ * the mapping).  Kept until a block lies beyond it or the allocator goes
+ * away; its pages are mapped in up front (MAP_POPULATE) -- only the used
+ * extent, not the file's sparse tail.  *base receives the mapping, NULL
+ * (with XMG_OK) when the allocator has no pagefile or no used page.
+ */
+int
+xmg_alloc_file_map(xm_allocator_t *a, const unsigned char **base)
+{
+	uint64_t p = a->path ? a->file_bytes / PAGE_BYTES : 0, need;
+	void *m;
+
+	*base = NULL;
+	while (p > 0 && !bit_get(a->used, p - 1))
+		p--;
+	need = p * PAGE_BYTES;
+	if (need == 0)
+		return XMG_OK;
+	if (a->map != NULL && a->map_bytes >= need) {
+		*base = a->map;
+		return XMG_OK;
+	}
+	if (a->map != NULL)
+		munmap((void *)a->map, a->map_bytes);
+	a->map = NULL;
+	a->map_bytes = 0;
+	m = mmap(NULL, need, PROT_READ, MAP_SHARED | MAP_POPULATE, a->fd, 0);
+	if (m == MAP_FAILED)
+		return xmg_seterr(XMG_EIO, "mmap of the pagefile failed");
+	a->map = m;
+	a->map_bytes = need;
+	*base = a->map;
+	return XMG_OK;
+}
+
+/* byte offset of a pagefile handle's data in the file */
+uint64_t
+xmg_alloc_file_offset(uint64_t h)
+{
+	return (uint64_t)page_offset(h);
+}
+
 void
 xm_allocator_destroy(xm_allocator_t *a)
 {
@@ -422,6 +472,8 @@ xm_allocator_destroy(xm_allocator_t *a)
 	if (a == NULL)
 		return;
 	xmg_adjoint_forget(a);
+	if (a->map != NULL)
+		munmap((void *)a->map, a->map_bytes);
 	if (a->path != NULL) {
 		xmg_alloc_release_views(a, 0);
 		if (close(a->fd))

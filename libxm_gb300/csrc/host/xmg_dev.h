@@ -49,6 +49,9 @@ int xmgd_side_sync(void);
 /* Copies between page-locked host memory and HBM on the side stream,
  * without a chunk slot (host-allocator blocks); xmgd_side_sync waits. */
 int xmgd_side_put(uint64_t dst, const void *src, size_t bytes);
+/* the device reads pageable host memory through the host's page tables
+ * (then side_put also takes pageable sources, at the link's rate) */
+int xmgd_pageable_direct(void);
 int xmgd_side_get(void *dst, uint64_t src, size_t bytes);
 size_t xmgd_arena_bytes_in_use(void);
 

@@ -56,6 +56,10 @@ int xmg_alloc_is_host(const xm_allocator_t *a);
 int xmg_alloc_device_view(xm_allocator_t *a, uint64_t handle, size_t bytes,
     uint64_t *dptr);
 int xmg_alloc_release_views(xm_allocator_t *a, int write_back);
+/* read-only mapping of a pagefile (NULL base for other allocators) and
+ * the file offset of a handle's data */
+int xmg_alloc_file_map(xm_allocator_t *a, const unsigned char **base);
+uint64_t xmg_alloc_file_offset(uint64_t h);
 
 /* tensor internals */
 struct xmg_block *xmg_tensor_block(const xm_tensor_t *t, xm_dim_t blkidx);

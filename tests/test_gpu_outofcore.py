@@ -1,8 +1,9 @@
 """GPU: out-of-core contractions with b streamed from the pagefile.
 
 With the staging budget forced to one byte, every pagefile contraction
-streams b through two HBM regions in batches (pinned chunks, side-stream
-copies overlapping the previous batch's contraction).  The regions are
+streams b through two HBM regions in batches (side-stream copies, from
+pinned chunks the reader threads fill or straight from the file's mapping,
+overlapping the previous batch's contraction).  The regions are
 made small so that the ladders split into many batches.  Results must
 match the oracle (in-memory tensors, same inputs) in both precision modes
 with alpha and beta applied exactly once, the out-of-core statistics must
@@ -42,8 +43,13 @@ def _copy_inputs(src, dst):
             td.write_block(blk, ts.read_block(blk))
 
 
+@pytest.mark.parametrize("mapped", ["0", "1"])
 @pytest.mark.parametrize("prec", [api.PREC_AUTO, api.PREC_FP64])
-def test_ladder_streamed(engine, oracle, staging, pagefile, prec):
+def test_ladder_streamed(engine, oracle, staging, pagefile, prec, mapped, monkeypatch):
+    """Both ways of reading the pagefile: reader threads through pinned
+    chunks (XMG_STAGE_MMAP=0) and copies straight from the file's mapping
+    (=1; the default where the device reads pageable host memory)."""
+    monkeypatch.setenv("XMG_STAGE_MMAP", mapped)
     engine.check(engine.xmg_set_precision(prec))
     oal = api.Allocator(oracle)
     we, wo = W.cfg1(engine, pagefile), W.cfg1(oracle, oal)
