@@ -240,8 +240,8 @@ void xmg_host_free(void *p);
  * when beta != 0) and b's first batch are copied in, then each further
  * batch of b is copied on a side stream while the previous batch is
  * contracted, and c is copied back before the call returns.  The batches
- * (about XMG_HOST_BATCHES of them, default 8, at most the staging region
- * each) grow by a factor XMG_HOST_GROWTH (default 1.2) from one to the
+ * (about XMG_HOST_BATCHES of them, default 6, at most the staging region
+ * each) grow by a factor XMG_HOST_GROWTH (default 1.15) from one to the
  * next, so that the first copy, which nothing overlaps, is short.  The
  * streamed plan of the last such contraction (batches, HBM regions, the
  * device plans and their graphs) is kept while the tensors' block

@@ -1530,17 +1530,19 @@ sp_match(const struct stream_plan *sp, xm_scalar_t alpha,
 	    strcmp(sp->idx[2], idxc) == 0;
 }
 
-/* host-allocator b: about XMG_HOST_BATCHES (default 8) batches growing
- * geometrically by XMG_HOST_GROWTH (default 1.2) per batch: the small
+/* host-allocator b: about XMG_HOST_BATCHES (default 6) batches growing
+ * geometrically by XMG_HOST_GROWTH (default 1.15) per batch: the small
  * first batch is the only copy nothing overlaps, and a batch's kernels
  * (for the FP64 ladders about 5-6 ms per GB of b) outlast the copy of the
  * next one (4.7 ms per GB over a 212 GB/s link) while the growth stays
- * below their ratio.  Returns the first batch's byte budget. */
+ * below their ratio (cfg2 ladder, measured: 6 batches at 1.15 57.4 ms per
+ * call, 8 at 1.2 58.3, 8 at 1.0 60.3, 4 at 1.0 60.7, 2 at 1.0 67.4).
+ * Returns the first batch's byte budget. */
 static double
 host_first_batch(uint64_t total, double *growth)
 {
 	const char *e = getenv("XMG_HOST_BATCHES"), *g = getenv("XMG_HOST_GROWTH");
-	double n = e ? atof(e) : 8, r = g ? atof(g) : 1.2;
+	double n = e ? atof(e) : 6, r = g ? atof(g) : 1.15;
 
 	if (n < 1)
 		n = 1;
