@@ -35,8 +35,8 @@
  *     warp 0 streams stages with cp.async.bulk, warp 1 issues the slice
  *     products per 16-wide K step with tcgen05.mma.kind::f16 (bf16 x bf16 ->
  *     fp32) into TMEM accumulators, warps 2..17 drain them every 256 K
- *     elements for FP64 and every <= 320 for FP32 (the exact groups stay
- *     below 3 * 320 * 2^14 < 2^24, exact in fp32) into
+ *     elements for FP64 and every <= 336 for FP32 (the exact groups stay
+ *     below 3 * 336 * 2^14 < 2^24, exact in fp32) into
  *     per-thread int64 fixed-point sums in units of 2^(-16-F), applying the
  *     pair factor exactly.  The epilogue is the only FP64 work:
  *     C = alpha * 2^(eA + eB - 2 * EXPOFF - 16 - F) * V + beta * C, scattered
@@ -362,19 +362,27 @@ __device__ __forceinline__ bool pack_f64(long long V, int e, unsigned long long 
 
 /* A pipeline stage holds KSTEPS consecutive 16-wide K steps (each the
  * M-side chunk then the N-side chunk).  The 3-slice form issues only 6
- * MMAs per K step, so it takes two steps per stage: the per-stage
- * synchronisation of the producer and MMA threads (barrier round trips,
- * copy issue, commit) would otherwise take longer than the step's MMAs
- * (measured: removing every copy, or every MMA, left the float32 GEMM
- * within 6 % of its time at one step per stage). */
+ * MMAs per K step, so it takes three steps per stage (three stages of 72
+ * KiB): the per-stage synchronisation of the producer and MMA threads
+ * (barrier round trips, copy issue, commit) would otherwise weigh on the
+ * step's MMAs (measured on the float32 ring term's GEMM: one step per
+ * stage 30.3-32.3 ms, two 27.8, three 27.0, four in two stages 26.5 with
+ * a one-stage head, 32.6 with two). */
 template <int S>
 struct stage_cfg {
-	static constexpr int KSTEPS = S == fin<float>::S ? 2 : 1;
+#ifndef EMU_KSTEPS32
+#define EMU_KSTEPS32 3
+#endif
+#ifndef EMU_BUDGET32
+#define EMU_BUDGET32 221184                   /* 3 stages of 72 KiB */
+#endif
+	static constexpr int KSTEPS = S == fin<float>::S ? EMU_KSTEPS32 : 1;
+	static constexpr int BUDGET = S == fin<float>::S ? EMU_BUDGET32 : STAGE_BUDGET;
 	static constexpr int CHUNK_BYTES = S * SLICE_BYTES;
 	static constexpr int STEP_BYTES = 2 * CHUNK_BYTES;
 	static constexpr int STAGE_BYTES = KSTEPS * STEP_BYTES;
-	static constexpr int NST = STAGE_BUDGET / STAGE_BYTES > 8 ? 8 :
-	    STAGE_BUDGET / STAGE_BYTES;
+	static constexpr int NST = BUDGET / STAGE_BYTES > 8 ? 8 :
+	    BUDGET / STAGE_BYTES;
 	static constexpr int SMEM = NST * STAGE_BYTES + 1024;
 };
 
@@ -411,10 +419,10 @@ __device__ __forceinline__ int stages_of(int nks, int cplx)
  * FP64 takes 256 (XMG_EMU_CHUNK steps, at most 20): its rounded low
  * band's error grows with the chunk (cfg2 ladder: 3.1e-13 at 160, 4.4e-13
  * at 224, 6.2e-13 at 320, against GEMM times of 35.8, 34.2 and 33.2 ms);
- * FP32, all exact, takes up to 20 steps (320), the steps left split into
- * equal chunks of whole stages (32 steps: 16 + 16, not 20 + 12), so that
- * the stages of a segment, which start at its first step, never straddle
- * a chunk boundary. */
+ * FP32, all exact, takes up to 20 steps, the steps left split into equal
+ * chunks rounded up to whole stages (at most 21 steps, 336 elements; 32
+ * steps: 18 + 14), so that the stages of a segment, which start at its
+ * first step, never straddle a chunk boundary. */
 template <int S>
 __device__ __forceinline__ int chunk_end(int c0, int nks, int cplx, int kchunk)
 {
@@ -1077,7 +1085,7 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 #pragma unroll
 						for (int c = 0; c < 4; c++) {
 							/* exact integers: with the pair factor's 2^1,
-							 * |i0| <= 2^14 * 320 * 2 < 2^23.4 and |i1| <
+							 * |i0| <= 2^14 * 336 * 2 < 2^23.4 and |i1| <
 							 * 2^24.4; the packing is 64-bit */
 							int i0 = __float2int_rn(a0[c] * sa);
 							int i1 = __float2int_rn(a1[c] * sb);
@@ -1714,10 +1722,10 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	e->cplx = cplx;
 	{
 		const int nst = dbl ? stage_cfg<fin<double>::S>::NST : stage_cfg<fin<float>::S>::NST;
-		/* head/tail length in stages: 4 one-step stages (FP64), 2
-		 * two-step stages (FP32) */
+		/* head/tail length in stages: 4 one-step stages (FP64), 1
+		 * three-step stage (FP32) */
 		const char *h = getenv("XMG_EMU_HEAD");
-		e->hmax = h ? atoi(h) : (dbl ? 4 : 2);
+		e->hmax = h ? atoi(h) : (dbl ? 4 : 1);
 		e->hmax = std::max(1, std::min(nst, e->hmax));
 		const char *kc = getenv("XMG_EMU_CHUNK");
 		e->kchunk = kc ? std::max(1, std::min(20, atoi(kc))) : EMU_CHUNK;
