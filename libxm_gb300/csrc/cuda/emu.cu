@@ -1040,15 +1040,27 @@ emu_gemm_kernel(const emu_item *__restrict__ items, int nitems,
 #pragma unroll
 						for (int c = 0; c < 4; c++) {
 							if (LOW) {
-								/* low band in units of 2^(-16-F) without a
-								 * 64-bit conversion: x = h * 2^24 + l with
-								 * h = rint(x / 2^24) and l = x - h * 2^24,
-								 * both exact in fp32 and converted as int32 */
+								/* low band in units of 2^(-16-F), rounded
+								 * to an integer with fp32 adds only (the
+								 * conversion pipe runs at 1/8 of the FMA
+								 * pipe's rate and bounded this drain):
+								 * x = h * 2^22 + l, h = rint(x / 2^22) read
+								 * from the bits of x / 2^22 + 1.5 * 2^23,
+								 * l = x - h * 2^22 exact (|l| <= 2^21) and
+								 * rounded the same way.  |x| < 2^42 (the
+								 * band is below 2 units of the leading
+								 * group per chunk, scaled by at most
+								 * 2^(16 + 24 + 1)), inside the 2^44 the
+								 * first add allows; the sum h * 2^22 +
+								 * rint(l) equals rint(x), ties to even,
+								 * as a direct conversion would give */
+								const float M = 12582912.0f;	/* 1.5 * 2^23 */
 								const float x = ax[c] * s3;
-								const float h = rintf(x * 5.9604644775390625e-8f);
-								const float l = fmaf(h, -16777216.0f, x);
-								V[b4 * 4 + c] += ((long long)__float2int_rn(h) << 24) +
-								    __float2int_rn(l);
+								const float t = fmaf(x, 2.384185791015625e-7f, M);
+								const float l = fmaf(t - M, -4194304.0f, x);
+								const int hi = __float_as_int(t) - 0x4B400000;
+								const int lo = __float_as_int(l + M) - 0x4B400000;
+								V[b4 * 4 + c] += ((long long)hi << 22) + lo;
 							} else {
 								V[b4 * 4 + c] += (long long)__float2int_rn(ax[c] * s2) << F;
 							}
