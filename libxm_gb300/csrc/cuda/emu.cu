@@ -361,13 +361,15 @@ __device__ __forceinline__ bool pack_f64(long long V, int e, unsigned long long 
 }
 
 /* A pipeline stage holds KSTEPS consecutive 16-wide K steps (each the
- * M-side chunk then the N-side chunk).  The 3-slice form issues only 6
- * MMAs per K step, so it takes three steps per stage (three stages of 72
- * KiB): the per-stage synchronisation of the producer and MMA threads
- * (barrier round trips, copy issue, commit) would otherwise weigh on the
- * step's MMAs (measured on the float32 ring term's GEMM: one step per
- * stage 30.3-32.3 ms, two 27.8, three 27.0, four in two stages 26.5 with
- * a one-stage head, 32.6 with two). */
+ * M-side chunk then the N-side chunk).  The per-stage synchronisation of
+ * the producer and MMA threads (barrier round trips, copy issue, commit)
+ * weighs on the stage's MMAs, so both forms take several steps per stage.
+ * The 3-slice form (6 MMAs per K step) three, in three stages of 72 KiB
+ * (measured on the float32 ring term's GEMM: one step per stage 30.3-32.3
+ * ms, two 27.8, three 27.0, four in two stages 26.5 with a one-stage head,
+ * 32.6 with two); the 6-slice form (21 MMAs per step) two, in two stages
+ * of 96 KiB (FP64 ring term 59.6 -> 56.5 ms, cfg2 ladder 32.4-32.9 ->
+ * 32.0 ms, with a head and tail of both stages). */
 template <int S>
 struct stage_cfg {
 #ifndef EMU_KSTEPS32
@@ -376,7 +378,10 @@ struct stage_cfg {
 #ifndef EMU_BUDGET32
 #define EMU_BUDGET32 221184                   /* 3 stages of 72 KiB */
 #endif
-	static constexpr int KSTEPS = S == fin<float>::S ? EMU_KSTEPS32 : 1;
+#ifndef EMU_KSTEPS64
+#define EMU_KSTEPS64 2                        /* 2 stages of 96 KiB */
+#endif
+	static constexpr int KSTEPS = S == fin<float>::S ? EMU_KSTEPS32 : EMU_KSTEPS64;
 	static constexpr int BUDGET = S == fin<float>::S ? EMU_BUDGET32 : STAGE_BUDGET;
 	static constexpr int CHUNK_BYTES = S * SLICE_BYTES;
 	static constexpr int STEP_BYTES = 2 * CHUNK_BYTES;
@@ -1734,13 +1739,17 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	e->cplx = cplx;
 	{
 		const int nst = dbl ? stage_cfg<fin<double>::S>::NST : stage_cfg<fin<float>::S>::NST;
-		/* head/tail length in stages: 4 one-step stages (FP64), 1
+		/* head/tail length in stages: 2 two-step stages (FP64), 1
 		 * three-step stage (FP32) */
 		const char *h = getenv("XMG_EMU_HEAD");
-		e->hmax = h ? atoi(h) : (dbl ? 4 : 1);
+		e->hmax = h ? atoi(h) : (dbl ? 2 : 1);
 		e->hmax = std::max(1, std::min(nst, e->hmax));
+		/* FP64 chunks in whole stages (they start at a segment's first
+		 * step, as the stages do) */
 		const char *kc = getenv("XMG_EMU_CHUNK");
+		constexpr int KS64 = stage_cfg<fin<double>::S>::KSTEPS;
 		e->kchunk = kc ? std::max(1, std::min(20, atoi(kc))) : EMU_CHUNK;
+		e->kchunk = std::max(KS64, e->kchunk / KS64 * KS64);
 		const char *f = getenv("XMG_EMU_PF");
 		e->pfd = f ? std::max(0, atoi(f)) : 0;
 	}
