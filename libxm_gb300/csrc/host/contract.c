@@ -759,6 +759,11 @@ struct io_job {
 	pthread_t th;
 	int running;
 	double ms;               /* wall time of the job (start to drained) */
+	/* host blocks: dst[0 .. seg) and dst[seg .. n) each lie in one device
+	 * buffer, so runs of blocks inside one part may be copied at once
+	 * (0: every block in its own allocation, one copy per block) */
+	size_t seg;
+	int merge;
 };
 
 /* one reader: chunks w, w + nw, w + 2 nw, ... of the list, alternating
@@ -826,18 +831,30 @@ stage_threads(void)
 	return n < 1 ? 1 : n > XMGD_SIDE_SLOTS / 2 ? XMGD_SIDE_SLOTS / 2 : n;
 }
 
-/* host-allocator blocks: one cudaMemcpyAsync per block straight from (or
- * into) the block's own page-locked memory, queued on the side stream */
+/* host-allocator blocks: cudaMemcpyAsync straight from (or into) the
+ * blocks' own page-locked memory, queued on the side stream.  When the job
+ * allows it (its device side lies in one or two buffers), one copy per run
+ * of blocks that lie at the same distances apart in host memory and in
+ * HBM (blocks carved one after another from a slab and placed one after
+ * another in a staging region: the usual case), since the copy engine
+ * moves few large copies faster than many block-sized ones; a run never
+ * spans two device buffers (a copy must stay inside one allocation) */
 static void
 io_host(struct io_job *j)
 {
-	size_t i;
+	size_t i, r;
 	int st = xmgd_bind_thread();
 
-	for (i = 0; st == XMG_OK && i < j->n; i++)
+	for (i = 0; st == XMG_OK && i < j->n; i = r) {
+		uint64_t end = j->h[i] + j->sz[i];
+		const size_t lim = !j->merge ? i + 1 : i < j->seg ? j->seg : j->n;
+		for (r = i + 1; r < lim && j->h[r] >= end &&
+		    j->h[r] - j->h[i] == j->dst[r] - j->dst[i]; r++)
+			end = j->h[r] + j->sz[r];
 		st = j->wr ? xmgd_side_get((void *)(uintptr_t)j->h[i], j->dst[i],
-		    j->sz[i]) : xmgd_side_put(j->dst[i],
-		    (const void *)(uintptr_t)j->h[i], j->sz[i]);
+		    end - j->h[i]) : xmgd_side_put(j->dst[i],
+		    (const void *)(uintptr_t)j->h[i], end - j->h[i]);
+	}
 	if (xmgd_side_sync() != XMG_OK && st == XMG_OK)
 		st = XMG_ECUDA;
 	if (st != XMG_OK)
@@ -1689,6 +1706,7 @@ sp_commit(struct stream_plan *sp, xm_tensor_t *c)
 	memset(&j, 0, sizeof j);
 	j.al = c->allocator;
 	j.h = sp->CH; j.sz = sp->CSZ; j.dst = sp->CD; j.n = sp->ncw; j.wr = 1;
+	j.merge = 1; j.seg = j.n;	/* c's views: one bulk buffer */
 	int st = io_start(&j);
 	return st == XMG_OK ? io_join(&j) : st;
 }
@@ -1734,6 +1752,8 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 	memcpy(JD + sp->nr, sp->D, n0 * sizeof *JD);
 	io[0].h = JH; io[0].sz = JSZ; io[0].dst = JD;
 	io[0].n = sp->nr + n0;
+	/* a's and c's views in the bulk buffer, then batch 0 in its region */
+	io[0].merge = 1; io[0].seg = sp->nr;
 	if ((st = io_start(&io[0])) != XMG_OK)
 		goto out;
 	for (k = 0; k < sp->nb && st == XMG_OK; k++) {
@@ -1785,6 +1805,7 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 			nx->sz = sp->SZ + sp->bstart[k + 1];
 			nx->dst = sp->D + sp->bstart[k + 1];
 			nx->n = sp->bstart[k + 2] - sp->bstart[k + 1];
+			nx->merge = 1; nx->seg = nx->n;	/* one region */
 			st = io_start(nx);
 		}
 		double tr0 = now_ms(), tw0 = tw;
