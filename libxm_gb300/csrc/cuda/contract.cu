@@ -39,6 +39,7 @@ int emu_policy(const emu_plan *e);
 int emu_current(const emu_plan *e);
 int emu_ncand(const emu_plan *e);
 bool emu_tuned(const emu_plan *e);
+int emu_a_mode(const emu_plan *e);
 void emu_free(emu_plan *e);
 
 static xmgd_timing_t g_timing;
@@ -410,6 +411,12 @@ xmgd_plan_run(xmgd_plan *dp, int *precision_used)
 			return st;
 	}
 	return check(cudaGetLastError(), "contraction kernels");
+}
+
+extern "C" int
+xmgd_plan_a_shared(const xmgd_plan *dp)
+{
+	return dp->ep && emu_a_mode(dp->ep) == 1;
 }
 
 extern "C" int

@@ -1285,6 +1285,8 @@ struct emu_plan {
 	int cur = 0, tuned = 0;
 	int hmax = 4;                        /* head/tail steps (<= stages) */
 	int pfd = 0;                         /* L2 prefetch distance, steps */
+	int a_mode = 0;                      /* shared a side (xmgd_contract_t) */
+	uint64_t a_slices = 0, a_E = 0, a_flag = 0;
 	int kchunk = EMU_CHUNK;              /* FP64: K steps per chunk */
 	uint64_t sig = 0;
 	int *h_flags = nullptr;              /* pinned: Inf/NaN, timeout */
@@ -1302,21 +1304,40 @@ launch_split(emu_plan *e)
 
 	XMG_CK(cudaMemsetAsync((void *)e->d_E, 0, (e->nE + 64) * sizeof(int32_t),
 	    stream()));
-	for (int side = 0; side < 2; side++) {
-		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
-		const int nv = (int)(side ? e->VB.size() : e->VA.size());
-		int32_t *E = side ? EB : EA;
-		if (e->nctas[side][0] > 0) {
-			emu_exp_kernel<TIN><<<(unsigned)e->nctas[side][0], 256, 0, stream()>>>(
-			    dv, (const view_meta *)e->d_meta[side][0], nv, e->d_tabs, E, flags);
-			g_launches++;
-			XMG_CK(cudaGetLastError());
+	/* a shared a side: the preparing plan fills the shared exponent table
+	 * and flag, every plan takes the flag's Inf/NaN bit into its own */
+	int *aflags = flags;
+	if (e->a_mode) {
+		EA = (int32_t *)e->a_E;
+		aflags = (int *)e->a_flag;
+		if (e->a_mode == 1) {
+			XMG_CK(cudaMemsetAsync(EA, 0, e->nexp_a * sizeof(int32_t), stream()));
+			XMG_CK(cudaMemsetAsync(aflags, 0, sizeof(int), stream()));
 		}
 	}
 	for (int side = 0; side < 2; side++) {
 		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
 		const int nv = (int)(side ? e->VB.size() : e->VA.size());
+		int32_t *E = side ? EB : EA;
+		if (side == 0 && e->a_mode == 2)
+			continue;
+		if (e->nctas[side][0] > 0) {
+			emu_exp_kernel<TIN><<<(unsigned)e->nctas[side][0], 256, 0, stream()>>>(
+			    dv, (const view_meta *)e->d_meta[side][0], nv, e->d_tabs, E,
+			    side ? flags : aflags);
+			g_launches++;
+			XMG_CK(cudaGetLastError());
+		}
+		if (side == 0 && e->a_mode)
+			XMG_CK(cudaMemcpyAsync(flags, aflags, sizeof(int),
+			    cudaMemcpyDeviceToDevice, stream()));
+	}
+	for (int side = 0; side < 2; side++) {
+		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
+		const int nv = (int)(side ? e->VB.size() : e->VA.size());
 		const int32_t *E = side ? EB : EA;
+		if (side == 0 && e->a_mode == 2)
+			continue;
 		if (e->nctas[side][1] > 0) {
 			emu_split_kernel<TIN><<<(unsigned)e->nctas[side][1], 256, 0, stream()>>>(
 			    dv, (const view_meta *)e->d_meta[side][1], nv, e->d_tabs, E);
@@ -1337,6 +1358,8 @@ launch_gemm(emu_plan *e)
 	const emu_cand &c = e->cand[e->cur];
 	int32_t *EA = (int32_t *)e->d_E, *EB = EA + e->nexp_a;
 	int *flags = (int *)(EA + e->nE);
+	if (e->a_mode)
+		EA = (int32_t *)e->a_E;	/* the shared a side's table */
 
 	if (pair_policy(c.policy)) {
 		/* clusters of two CTAs */
@@ -1760,7 +1783,12 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 	e->d_tabs = d_tabs;
 	e->VA.assign(p->views_a, p->views_a + p->nviews_a);
 	e->VB.assign(p->views_b, p->views_b + p->nviews_b);
-	e->useA.assign(e->VA.size(), 0);
+	/* the plan that prepares a shared a side splits every view of a */
+	e->a_mode = p->a_mode;
+	e->a_slices = p->a_slices;
+	e->a_E = p->a_E;
+	e->a_flag = p->a_flag;
+	e->useA.assign(e->VA.size(), p->a_mode == 1);
 	e->useB.assign(e->VB.size(), 0);
 	e->split = dbl ? launch_split<double> : launch_split<float>;
 	e->gemm = dbl ? launch_gemm<double, double> : launch_gemm<float, float>;
@@ -1800,7 +1828,8 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 
 	/* slice storage: offsets now, rebased onto the workspace at bind */
 	size_t off = 0;
-	auto tile = [&](std::vector<xmgd_view_t> &V, std::vector<char> &use) {
+	auto tile = [&](std::vector<xmgd_view_t> &V, std::vector<char> &use,
+	    const int64_t *ext) {
 		for (size_t v = 0; v < V.size(); v++) {
 			if (!use[v])
 				continue;
@@ -1813,12 +1842,16 @@ emu_prepare(const xmgd_contract_t *p, const std::vector<int> &cblocks,
 			w.kcontig = w.kfast;
 			for (int32_t k = 2; w.kcontig && k < w.k; k++)
 				w.kcontig = p->tabs[w.rowtab + k] - p->tabs[w.rowtab] == k;
+			if (ext) {	/* in the shared a side's buffer */
+				w.slices = (uint64_t)ext[v];
+				continue;
+			}
 			w.slices = off;
 			off += (size_t)w.n_rt * w.n_ks * chunk_bytes;
 		}
 	};
-	tile(e->VA, e->useA);
-	tile(e->VB, e->useB);
+	tile(e->VA, e->useA, p->a_mode ? p->a_off : nullptr);
+	tile(e->VB, e->useB, nullptr);
 	e->slice_bytes = off;
 
 	/* CTA ranges of the exponent and split launches of each side */
@@ -1941,9 +1974,10 @@ emu_bind(emu_plan *e, bool *moved)
 	for (int side = 0; side < 2; side++) {
 		std::vector<xmgd_view_t> V = side ? e->VB : e->VA;
 		std::vector<char> &use = side ? e->useB : e->useA;
+		const uint64_t base = side == 0 && e->a_mode ? e->a_slices : ws;
 		for (size_t v = 0; v < V.size(); v++)
 			if (use[v])
-				V[v].slices += ws;
+				V[v].slices += base;
 		XMG_CK(cudaMemcpyAsync((void *)(side ? e->d_vb : e->d_va), V.data(),
 		    V.size() * sizeof(xmgd_view_t), cudaMemcpyHostToDevice, stream()));
 		XMG_CK(cudaStreamSynchronize(stream()));
@@ -1992,6 +2026,21 @@ bool emu_tuned(const emu_plan *e) { return e->tuned != 0; }
 int emu_record_split(emu_plan *e) { return e->split(e); }
 int emu_record_gemm(emu_plan *e) { return e->gemm(e); }
 int64_t emu_slice_bytes(const emu_plan *e) { return (int64_t)e->slice_bytes; }
+int emu_a_mode(const emu_plan *e) { return e->a_mode; }
+
+/* the slice bytes tile() gives one view */
+extern "C" int64_t
+xmgd_emu_view_bytes(const xmgd_view_t *v, int dtype)
+{
+	if (dtype < 0 || dtype > 3)
+		return 0;
+	const bool cplx = dtype == 1 || dtype == 3;
+	const int chunk_bytes = (dtype >= 2 ? fin<double>::S : fin<float>::S) *
+	    SLICE_BYTES;
+	const int64_t n_rt = (v->mn + EMU_TM - 1) / EMU_TM;
+	const int64_t n_ks = (cplx ? 2 : 1) * ((v->k + EMU_KS - 1) / EMU_KS);
+	return n_rt * n_ks * chunk_bytes;
+}
 int emu_items(const emu_plan *e) { return e->cand[e->cur].nitems; }
 int emu_policy(const emu_plan *e) { return e->cand[e->cur].policy; }
 

@@ -1252,7 +1252,7 @@ form_batches(const struct hsz *u, size_t nu, size_t region, double first,
 static int
 batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xmg_hmap_t *al,
     struct batch_buf *bb, xm_scalar_t alpha, xm_scalar_t beta, int prec,
-    xmgd_contract_t *dp)
+    int all_a, xmgd_contract_t *dp)
 {
 	const double mult = xmg_is_complex(pf->type) ? 8.0 : 2.0;
 	double flops = 0;
@@ -1296,6 +1296,16 @@ batch_plan(const plan_t *pf, const xmg_hmap_t *dmap, const xmg_hmap_t *al,
 			flops += mult * cs->m * (double)cs->n * ps->k;
 		}
 		cd->npairs = npr - cd->first_pair;
+	}
+	/* all_a: every view of a, the ones no pair of the batch uses last */
+	for (v = 0; all_a && v < pf->nva; v++) {
+		if (bb->vamap[v] >= 0)
+			continue;
+		bb->va[nva] = pf->va[v];
+		if ((bb->va[nva].ptr = handle_addr(al, pf->va[v].ptr)) == 0)
+			return xmg_seterr(XMG_EINVAL, "xm_contract: a block of a "
+			    "without a staged view");
+		bb->vamap[v] = nva++;
 	}
 	memset(dp, 0, sizeof *dp);
 	dp->dtype = pf->type;
@@ -1409,7 +1419,7 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 		for (i = bstart[k]; i < bstart[k + 1]; i++)
 			if (xmg_hmap_put(&dmap, u[i].h, u[i].h))
 				xm_fatal("%s: out of memory", __func__);
-		if ((st = batch_plan(&p, &dmap, NULL, &bb, 1, k == 0 ? 0 : 1,
+		if ((st = batch_plan(&p, &dmap, NULL, &bb, 1, k == 0 ? 0 : 1, 0,
 		    XMG_PREC_EMU64, &dp)) != XMG_OK)
 			break;
 		/* each pair of the batch is a later pair of its output block
@@ -1498,6 +1508,10 @@ struct stream_plan {
 	size_t nr, ncw;
 	uint64_t *RH, *RSZ, *RD, *CH, *CSZ, *CD;
 	xmg_hmap_t vmap;            /* a's and c's handles -> addresses */
+	/* a's split-precision operands, prepared by batch 0 for the later
+	 * batches (a_share 1): slices, exponent table, Inf/NaN flag in abuf */
+	uint64_t abuf;
+	int a_share;
 	xmgd_plan_t **bp;           /* per batch, built on first use */
 	double *bflops;
 	int *bnpairs;
@@ -1525,6 +1539,8 @@ sp_free(struct stream_plan *sp)
 		xmgd_free(sp->reg[1]);
 	if (sp->bulk)
 		xmgd_free(sp->bulk);
+	if (sp->abuf)
+		xmgd_free(sp->abuf);
 	xmg_hmap_free(&sp->vmap);
 	free(sp->bstart); free(sp->H); free(sp->SZ); free(sp->D);
 	free(sp->RH); free(sp->RSZ); free(sp->RD);
@@ -1712,6 +1728,49 @@ sp_commit(struct stream_plan *sp, xm_tensor_t *c)
 }
 
 /*
+ * a's split-precision operands once per call instead of once per batch:
+ * batch 0's plan splits every view of a into one buffer of the stream
+ * plan, the later batches' plans read them there.  XMG_STREAM_SHARE_A=0
+ * splits a in every batch.  *off gets each view's slice offset (whole
+ * plan's view ids); returns the slice bytes, 0 when a is not shared.
+ */
+static uint64_t
+a_side_offsets(const struct stream_plan *sp, const plan_t *p0, int64_t *off)
+{
+	const char *e = getenv("XMG_STREAM_SHARE_A");
+	uint64_t tot = 0;
+	int v;
+
+	if (sp->nb < 2 || sp->precision == XMG_PREC_FP64 || (int)p0->type < 0 ||
+	    (int)p0->type > 3 || (e && strcmp(e, "0") == 0))
+		return 0;
+	for (v = 0; v < p0->nva; v++) {
+		off[v] = (int64_t)tot;
+		tot += (uint64_t)xmgd_emu_view_bytes(&p0->va[v], p0->type);
+	}
+	return tot;
+}
+
+/* the shared a side of batch k's plan: batch 0 prepares it (its views
+ * are all of a's), the others use it */
+static void
+a_side_attach(const struct stream_plan *sp, const plan_t *p0,
+    const struct batch_buf *bb, const int64_t *offg, uint64_t slice_bytes,
+    size_t k, int64_t *offl, xmgd_contract_t *dp)
+{
+	int v;
+
+	for (v = 0; v < p0->nva; v++)
+		if (bb->vamap[v] >= 0)
+			offl[bb->vamap[v]] = offg[v];
+	dp->a_mode = k == 0 ? 1 : 2;
+	dp->a_slices = sp->abuf;
+	dp->a_E = sp->abuf + slice_bytes;
+	dp->a_flag = dp->a_E + ((uint64_t)p0->nexp_a * 4 + 15) / 16 * 16;
+	dp->a_off = offl;
+}
+
+/*
  * One call of a streamed contraction: a's (and, for beta != 0, c's)
  * blocks and batch 0 are read while batch 0's plan is built (on the
  * first call), then batch k + 1 streams into the idle region while batch
@@ -1723,7 +1782,8 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 {
 	struct batch_buf bb = {NULL, NULL, NULL, NULL, NULL, NULL};
 	struct io_job io[2];
-	uint64_t *JH = NULL, *JSZ = NULL, *JD = NULL;
+	uint64_t *JH = NULL, *JSZ = NULL, *JD = NULL, abytes = 0;
+	int64_t *offg = NULL, *offl = NULL;
 	xmg_hmap_t filt;
 	xmg_stats_t acc;
 	size_t i, k, n0 = sp->bstart[1];
@@ -1768,8 +1828,22 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 				    "plan without its batch plans");
 				break;
 			}
-			if (bb.cb == NULL)
+			if (bb.cb == NULL) {
 				batch_buf_alloc(&bb, p0);
+				offg = malloc((p0->nva + 1) * sizeof *offg);
+				offl = malloc((p0->nva + 1) * sizeof *offl);
+				if (!offg || !offl)
+					xm_fatal("%s: out of memory", __func__);
+			}
+			/* a's operands shared: laid out and allocated with
+			 * batch 0's plan */
+			if (k == 0 && (abytes = a_side_offsets(sp, p0, offg)) > 0) {
+				uint64_t eb = ((uint64_t)p0->nexp_a * 4 + 15) / 16 * 16;
+				if (sp->abuf == 0 && (st = xmgd_alloc(abytes + eb + 16,
+				    &sp->abuf)) != XMG_OK)
+					break;
+				sp->a_share = 1;
+			}
 			/* the batch's blocks resolve into its region */
 			xmg_hmap_free(&filt);
 			xmg_hmap_init(&filt);
@@ -1777,13 +1851,22 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 				if (xmg_hmap_put(&filt, sp->H[i], sp->D[i]))
 					xm_fatal("%s: out of memory", __func__);
 			if ((st = batch_plan(p0, &filt, &sp->vmap, &bb, sp->alpha,
-			    k == 0 ? sp->beta : 1, sp->precision, &dp)) == XMG_OK) {
+			    k == 0 ? sp->beta : 1, sp->precision,
+			    k == 0 && sp->a_share, &dp)) == XMG_OK) {
+				if (sp->a_share)
+					a_side_attach(sp, p0, &bb, offg, abytes, k,
+					    offl, &dp);
 				/* a kept plan is replayed: graphs and tuning */
 				dp.one_shot = !sp->keep;
 				st = xmgd_plan_create(&dp, &sp->bp[k]);
 				sp->bflops[k] = dp.flops;
 				sp->bnpairs[k] = dp.npairs;
 			}
+			/* batch 0 without a split-precision part prepares
+			 * nothing: the others split a themselves */
+			if (st == XMG_OK && k == 0 && sp->a_share &&
+			    !xmgd_plan_a_shared(sp->bp[0]))
+				sp->a_share = 0;
 		}
 		acc.ms_plan += now_ms() - t0;
 		/* batch k's data in place (only batch 0 can still be loading:
@@ -1863,6 +1946,7 @@ out:
 	xmg_hmap_free(&filt);
 	batch_buf_free(&bb);
 	free(JH); free(JSZ); free(JD);
+	free(offg); free(offl);
 	return st;
 }
 

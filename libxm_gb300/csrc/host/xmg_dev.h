@@ -150,7 +150,18 @@ typedef struct {
 	int precision_used;          /* out: XMG_PREC_FP64 / XMG_PREC_EMU64 */
 	int one_shot;                /* the plan runs once (an out-of-core
 	                                batch): no graphs, no tuning runs */
+	/* a's split-precision operands shared by the batches of a streamed
+	 * contraction: 0 none; 1 this plan prepares them for all of a's views
+	 * (exponent table a_E, slices in a_slices at a_off[v] for view v,
+	 * Inf/NaN flag a_flag); 2 this plan uses them as prepared */
+	int a_mode;
+	uint64_t a_slices, a_E, a_flag;
+	const int64_t *a_off;
 } xmgd_contract_t;
+
+/* bytes of one operand view's split-precision slices in a contraction of
+ * scalar type dtype (0 when the type has no split-precision form) */
+int64_t xmgd_emu_view_bytes(const xmgd_view_t *v, int dtype);
 
 int xmgd_contract(xmgd_contract_t *plan);
 /* the split-precision work list of one policy, built and checked on the
@@ -165,6 +176,9 @@ typedef struct xmgd_plan xmgd_plan_t;
 int xmgd_plan_create(const xmgd_contract_t *p, xmgd_plan_t **out);
 int xmgd_plan_run(xmgd_plan_t *dp, int *precision_used);
 void xmgd_plan_free(xmgd_plan_t *dp);
+/* 1 when the plan prepares a shared a side (a_mode 1 and a
+ * split-precision part that took it) */
+int xmgd_plan_a_shared(const xmgd_plan_t *dp);
 
 /* Timing of the last xmgd_contract, milliseconds (device events). */
 typedef struct {

@@ -140,6 +140,51 @@ def test_kept_streamed_plan(engine, oracle, hal, oal):
         wo.free()
 
 
+def test_shared_a_side(engine, oracle, hal, oal, monkeypatch):
+    """a's split-precision operands prepared once per call by batch 0 and
+    read by the later batches (XMG_STREAM_SHARE_A=1, the default) give the
+    oracle's result as splitting a in every batch does, on replays of the
+    kept plan too, with less slice workspace; an Inf in a reaches every
+    batch (all of them fall back to FP64) and clean data brings the
+    split-precision path back."""
+    slice_bytes = {}
+    for share in ("0", "1"):
+        monkeypatch.setenv("XMG_STREAM_SHARE_A", share)
+        we, wo = W.cfg2(engine, hal, scale=4), W.cfg2(oracle, oal, scale=4)
+        try:
+            for w in (we, wo):
+                W.fill(w.c, 37, W.LADDER_ANTISYM)
+                w.alpha, w.beta = 0.9, 0.25
+            for _ in range(2):
+                we.run()
+                wo.run()
+                st = api.last_stats(engine)
+                assert st.stage_batches > 1
+                assert st.precision_used == api.PREC_EMU64
+                assert W.rel_frobenius(W.read_canonical(we.c), W.read_canonical(wo.c)) <= REL
+            slice_bytes[share] = st.slice_bytes
+            for w in (we, wo):
+                blk = w.a.canonical_blocks()[0]
+                x = w.a.read_block(blk)
+                x.flat[0] = np.inf
+                w.a.write_block(blk, x)
+                w.run()
+            assert api.last_stats(engine).precision_used == api.PREC_FP64
+            got, ref = W.read_canonical(we.c), W.read_canonical(wo.c)
+            for k in ref:
+                np.testing.assert_allclose(got[k], ref[k], rtol=1e-10, atol=1e-10)
+            for w in (we, wo):
+                W.fill(w.a, 38, W.LADDER_ANTISYM)
+                W.fill(w.c, 39, W.LADDER_ANTISYM)
+                w.run()
+            assert api.last_stats(engine).precision_used == api.PREC_EMU64
+            assert W.rel_frobenius(W.read_canonical(we.c), W.read_canonical(wo.c)) <= REL
+        finally:
+            we.free()
+            wo.free()
+    assert slice_bytes["1"] < slice_bytes["0"], slice_bytes
+
+
 def test_elementwise_host_memory(engine, oracle, hal, oal):
     """xm_set, xm_add with a permutation, xm_dot on host-memory tensors."""
     for dt in (api.DOUBLE, api.FLOAT_COMPLEX):
