@@ -80,17 +80,28 @@ int xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
     const char *idxc, int policy, long long out[4]);
 
 /* The out-of-core batch plans, cut on the host without a device from the
- * whole plan, for b's blocks (in file order) in the streamed path's
- * batches of at most `region` bytes, or, with region <= 0, in nbatch
- * equal runs: out = {batches, pairs over all batches, work-list items of
- * `policy` over all batches, 1 if every block lies aligned inside its
- * batch's region after the previous one, every pair of the whole plan is
- * in exactly one batch, in its order, with its views, the flops add up and
- * every batch's work list holds its invariants}.  For tests. */
+ * whole plan, for b's blocks (in the streamed path's order: file order,
+ * or the order of the output blocks they feed under
+ * XMG_STREAM_ORDER=output) in the
+ * streamed path's batches of at most `region` bytes, or, with region <= 0,
+ * in nbatch equal runs: out = {batches, pairs over all batches, work-list
+ * items of `policy` over all batches, 1 if every block lies aligned inside
+ * its batch's region after the previous one, every pair of the whole plan
+ * is in exactly one batch, in its order, with its views, the flops add up,
+ * every batch's work list holds its invariants and no block of c is
+ * written back before the last batch that feeds it}.  For tests. */
 int xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
     const xm_tensor_t *c, const char *idxa, const char *idxb,
     const char *idxc, int nbatch, long long region, int policy,
     long long out[4]);
+
+/* The copies the staging path makes for a list of n blocks (host address
+ * h[i], bytes sz[i], device address dst[i]): one per run of blocks that
+ * follow one another on both sides with only alignment padding between;
+ * start[q] = the first block of run q (start holds n entries).  Returns
+ * the number of runs.  For tests. */
+size_t xmg_copy_runs(const uint64_t *h, const uint64_t *sz,
+    const uint64_t *dst, size_t n, size_t *start);
 
 /* Statistics of the last xm_contract / xmg_contract on this process. */
 typedef struct {
@@ -122,9 +133,17 @@ int xmg_get_last_stats(xmg_stats_t *out);
  * memory through the host's page tables (a coherent CPU-GPU link) the
  * copies read the pagefile's blocks straight from a read-only mapping of
  * the file, else reader threads read them into pinned chunks first
- * (XMG_STAGE_MMAP=0 / 1 forces either).  a and c are staged whole.  Defaults: 180 GB and 32 GB,
- * or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps the current
- * value. */
+ * (XMG_STAGE_MMAP=0 / 1 forces either).  a and c are staged whole; a's
+ * split-precision operands are prepared once per call, by the first
+ * batch, for all batches (XMG_STREAM_SHARE_A=0: in every batch).  Each
+ * block of c goes back to the host as soon as the last batch that feeds
+ * it has run, while later batches run (XMG_STREAM_CWRITE=0: all of c
+ * after the last batch; with reader threads staging b, always after the
+ * last batch).  b's blocks are batched in file order, or in the order of
+ * the output blocks they feed with XMG_STREAM_ORDER=output (each batch
+ * then feeds a range of c's blocks, which go back early).  Defaults: 180
+ * GB and 32 GB, or XMG_STAGE_BUDGET_GB / XMG_STAGE_REGION_GB; 0 keeps the
+ * current value. */
 int xmg_set_staging(size_t budget, size_t region);
 
 /* Hand-written adjoint of c = alpha * a * b over the index strings.  Given
@@ -239,7 +258,8 @@ void xmg_host_free(void *p);
  * operands of such tensors through HBM on every call: a's blocks (and c's
  * when beta != 0) and b's first batch are copied in, then each further
  * batch of b is copied on a side stream while the previous batch is
- * contracted, and c is copied back before the call returns.  The batches
+ * contracted, and c is copied back before the call returns (block by
+ * block once final, as for the pagefile).  The batches
  * (about XMG_HOST_BATCHES of them, default 6, at most the staging region
  * each) grow by a factor XMG_HOST_GROWTH (default 1.15) from one to the
  * next, so that the first copy, which nothing overlaps, is short.  The

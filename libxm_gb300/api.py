@@ -128,6 +128,9 @@ _GB_SIGS = {
     "xmg_batch_plan_check": (C.c_int, [_P, _P, _P, C.c_char_p, C.c_char_p, C.c_char_p,
                                        C.c_int, C.c_longlong, C.c_int,
                                        C.POINTER(C.c_longlong)]),
+    "xmg_copy_runs": (C.c_size_t, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_uint64), C.c_size_t,
+                                   C.POINTER(C.c_size_t)]),
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
     "xmg_plan_cache_clear": (None, []),

@@ -1319,15 +1319,15 @@ launch_split(emu_plan *e)
 		const xmgd_view_t *dv = (const xmgd_view_t *)(side ? e->d_vb : e->d_va);
 		const int nv = (int)(side ? e->VB.size() : e->VA.size());
 		int32_t *E = side ? EB : EA;
-		if (side == 0 && e->a_mode == 2)
-			continue;
-		if (e->nctas[side][0] > 0) {
+		if (e->nctas[side][0] > 0 && !(side == 0 && e->a_mode == 2)) {
 			emu_exp_kernel<TIN><<<(unsigned)e->nctas[side][0], 256, 0, stream()>>>(
 			    dv, (const view_meta *)e->d_meta[side][0], nv, e->d_tabs, E,
 			    side ? flags : aflags);
 			g_launches++;
 			XMG_CK(cudaGetLastError());
 		}
+		/* every plan of a shared a side, the preparing one and the
+		 * ones that use it, takes its Inf/NaN bit */
 		if (side == 0 && e->a_mode)
 			XMG_CK(cudaMemcpyAsync(flags, aflags, sizeof(int),
 			    cudaMemcpyDeviceToDevice, stream()));

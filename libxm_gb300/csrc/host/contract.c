@@ -831,14 +831,46 @@ stage_threads(void)
 	return n < 1 ? 1 : n > XMGD_SIDE_SLOTS / 2 ? XMGD_SIDE_SLOTS / 2 : n;
 }
 
+/* The end of the run of blocks i, i + 1, ... (below lim) that one copy
+ * may move: block r joins when it follows block r - 1 at the same distance
+ * in host memory and in HBM with less than one alignment unit between
+ * them.  Blocks start 256-byte aligned on both sides, so only padding lies
+ * inside a run, never another block (equal end-to-end distances alone
+ * would let two equal-sized blocks trade places). */
+static size_t
+copy_run_end(const uint64_t *h, const uint64_t *sz, const uint64_t *dst,
+    size_t i, size_t lim)
+{
+	uint64_t end = h[i] + sz[i];
+	size_t r;
+
+	for (r = i + 1; r < lim && h[r] >= end && h[r] - end < STAGE_ALIGN &&
+	    h[r] - h[r - 1] == dst[r] - dst[r - 1]; r++)
+		end = h[r] + sz[r];
+	return r;
+}
+
+/* the runs copy_run_end forms over a list (host-side check): run q starts
+ * at block start[q]; returns the number of runs */
+size_t
+xmg_copy_runs(const uint64_t *h, const uint64_t *sz, const uint64_t *dst,
+    size_t n, size_t *start)
+{
+	size_t i, q = 0;
+
+	for (i = 0; i < n; i = copy_run_end(h, sz, dst, i, n))
+		start[q++] = i;
+	return q;
+}
+
 /* host-allocator blocks: cudaMemcpyAsync straight from (or into) the
  * blocks' own page-locked memory, queued on the side stream.  When the job
  * allows it (its device side lies in one or two buffers), one copy per run
- * of blocks that lie at the same distances apart in host memory and in
- * HBM (blocks carved one after another from a slab and placed one after
- * another in a staging region: the usual case), since the copy engine
- * moves few large copies faster than many block-sized ones; a run never
- * spans two device buffers (a copy must stay inside one allocation) */
+ * of blocks that follow one another in host memory and in HBM (blocks
+ * carved one after another from a slab and placed one after another in a
+ * staging region: the usual case), since the copy engine moves few large
+ * copies faster than many block-sized ones; a run never spans two device
+ * buffers (a copy must stay inside one allocation) */
 static void
 io_host(struct io_job *j)
 {
@@ -846,11 +878,9 @@ io_host(struct io_job *j)
 	int st = xmgd_bind_thread();
 
 	for (i = 0; st == XMG_OK && i < j->n; i = r) {
-		uint64_t end = j->h[i] + j->sz[i];
 		const size_t lim = !j->merge ? i + 1 : i < j->seg ? j->seg : j->n;
-		for (r = i + 1; r < lim && j->h[r] >= end &&
-		    j->h[r] - j->h[i] == j->dst[r] - j->dst[i]; r++)
-			end = j->h[r] + j->sz[r];
+		r = copy_run_end(j->h, j->sz, j->dst, i, lim);
+		const uint64_t end = j->h[r - 1] + j->sz[r - 1];
 		st = j->wr ? xmgd_side_get((void *)(uintptr_t)j->h[i], j->dst[i],
 		    end - j->h[i]) : xmgd_side_put(j->dst[i],
 		    (const void *)(uintptr_t)j->h[i], end - j->h[i]);
@@ -975,7 +1005,18 @@ io_join(struct io_job *j)
 
 struct hsz {
 	uint64_t h, sz;
+	int64_t key;             /* ordering key (order_by_output) */
 };
+
+static int
+cmp_key(const void *x, const void *y)
+{
+	const struct hsz *p = x, *q = y;
+
+	if (p->key != q->key)
+		return p->key < q->key ? -1 : 1;
+	return p->h < q->h ? -1 : p->h > q->h;
+}
 
 static int
 cmp_hsz(const void *x, const void *y)
@@ -1198,6 +1239,7 @@ distinct_b(const plan_t *p, struct hsz **out)
 	for (i = 0; i < p->nbh; i++) {
 		u[i].h = p->bh[i];
 		u[i].sz = p->bsz[i];
+		u[i].key = 0;
 	}
 	if (p->nbh)
 		qsort(u, p->nbh, sizeof *u, cmp_hsz);
@@ -1247,6 +1289,121 @@ form_batches(const struct hsz *u, size_t nu, size_t region, double first,
 	}
 	bstart[*nb] = nu;
 	return XMG_OK;
+}
+
+/* XMG_STREAM_ORDER=output cuts b's batches in the output blocks' order
+ * (order_by_output) instead of file order.  Not the default: where b's
+ * contracted indices lead (the ladders' "cdab"), a batch in output order
+ * is a block from every run of the file, its copies no longer merge, and
+ * on a GB300 the host link moved such batches at ~147 GB/s against ~212
+ * for merged ones, while the kernels ran no faster (cfg2 from host
+ * memory: 53.8 ms per call against 52.3 in file order). */
+static int
+stream_order_output(void)
+{
+	const char *e = getenv("XMG_STREAM_ORDER");
+
+	return e && strcmp(e, "output") == 0;
+}
+
+/*
+ * b's distinct blocks in the order of the output blocks they feed: by the
+ * smallest b-side exponent slot (one per b-side free block index of c)
+ * among the pairs that read the block, then by handle.  Batches cut on
+ * this order each feed a range of c's blocks, so a block of c is final
+ * once the batch holding its last pair has run (and may go back to the
+ * host while later batches run), and each batch's kernels read and
+ * write only its range of c.  In file order, with b's contracted indices
+ * leading, every batch feeds every block of c.
+ */
+static void
+order_by_output(const plan_t *p, struct hsz *u, size_t nu)
+{
+	xmg_hmap_t ix;
+	uint64_t v;
+	size_t i;
+	int l, q;
+
+	xmg_hmap_init(&ix);
+	for (i = 0; i < nu; i++) {
+		u[i].key = INT64_MAX;
+		if (xmg_hmap_put(&ix, u[i].h, i))
+			xm_fatal("%s: out of memory", __func__);
+	}
+	for (l = 0; l < p->ncb; l++) {
+		const xmgd_cblock_t *cb = &p->cb[l];
+		for (q = 0; q < cb->npairs; q++)
+			if (xmg_hmap_get(&ix, p->pr[cb->first_pair + q].b_ptr, &v) &&
+			    cb->eB < u[v].key)
+				u[v].key = cb->eB;
+	}
+	xmg_hmap_free(&ix);
+	if (nu)
+		qsort(u, nu, sizeof *u, cmp_key);
+}
+
+/*
+ * c's canonical blocks (ch, csz, cd; n of them) reordered by the batch
+ * after which each is final: the batch of its last pair, batch 0 for a
+ * block without pairs (only beta applies, in batch 0), the last batch for
+ * a block the plan does not list.  cstart[k] .. cstart[k + 1] - 1 are the
+ * blocks final after batch k.
+ */
+static void
+c_by_last_batch(const plan_t *p, const uint64_t *H, const size_t *bstart,
+    size_t nb, uint64_t *ch, uint64_t *csz, uint64_t *cd, size_t n,
+    size_t *cstart)
+{
+	xmg_hmap_t bk, ck;
+	uint64_t v, *t;
+	size_t i, k, *last, *pos;
+	int l, q;
+
+	xmg_hmap_init(&bk);
+	xmg_hmap_init(&ck);
+	for (k = 0; k < nb; k++)
+		for (i = bstart[k]; i < bstart[k + 1]; i++)
+			if (xmg_hmap_put(&bk, H[i], k))
+				xm_fatal("%s: out of memory", __func__);
+	for (l = 0; l < p->ncb; l++) {
+		const xmgd_cblock_t *cb = &p->cb[l];
+		uint64_t lb = 0;
+		for (q = 0; q < cb->npairs; q++)
+			if (xmg_hmap_get(&bk, p->pr[cb->first_pair + q].b_ptr, &v) &&
+			    v > lb)
+				lb = v;
+		if (xmg_hmap_get(&ck, cb->c_ptr, &v) && v > lb)
+			lb = v;
+		if (xmg_hmap_put(&ck, cb->c_ptr, lb))
+			xm_fatal("%s: out of memory", __func__);
+	}
+	last = malloc((n + 1) * sizeof *last);
+	pos = calloc(nb + 1, sizeof *pos);
+	t = malloc((n + 1) * sizeof *t);
+	if (!last || !pos || !t)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < n; i++) {
+		last[i] = xmg_hmap_get(&ck, ch[i], &v) ? (size_t)v : nb - 1;
+		pos[last[i] + 1]++;
+	}
+	for (k = 0; k < nb; k++)
+		pos[k + 1] += pos[k];
+	memcpy(cstart, pos, (nb + 1) * sizeof *cstart);
+	/* a stable counting sort of the three arrays */
+	uint64_t *arr[3] = {ch, csz, cd};
+	for (int a = 0; a < 3; a++) {
+		size_t *at = malloc((nb + 1) * sizeof *at);
+		if (!at)
+			xm_fatal("%s: out of memory", __func__);
+		memcpy(at, cstart, (nb + 1) * sizeof *at);
+		for (i = 0; i < n; i++)
+			t[at[last[i]]++] = arr[a][i];
+		memcpy(arr[a], t, n * sizeof *t);
+		free(at);
+	}
+	free(last); free(pos); free(t);
+	xmg_hmap_free(&bk);
+	xmg_hmap_free(&ck);
 }
 
 static int
@@ -1368,8 +1525,10 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 	unsigned char *used = NULL;
 	double flops = 0;
 	long long wl[4], npairs = 0, items = 0;
-	uint64_t *off = NULL, rbytes;
-	size_t nu, i, k, *bstart = NULL, nb;
+	uint64_t *off = NULL, rbytes, *H = NULL, *ch = NULL, *cz = NULL,
+	    *cd0 = NULL, fv;
+	size_t nu, i, k, *bstart = NULL, nb, *cstart = NULL;
+	xmg_hmap_t fin;
 	int st, l, j, q, ok = 1;
 
 	memset(out, 0, 4 * sizeof *out);
@@ -1383,6 +1542,8 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 		return st;
 	}
 	nu = distinct_b(&p, &u);
+	if (stream_order_output())
+		order_by_output(&p, u, nu);
 	batch_buf_alloc(&bb, &p);
 	used = calloc(p.npr + 1, 1);
 	off = malloc((nu + 1) * sizeof *off);
@@ -1412,6 +1573,24 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 		for (k = 0; k <= nb; k++)
 			bstart[k] = nu * k / nb;
 	}
+	/* c's blocks by the batch after which they are final */
+	xmg_hmap_init(&fin);
+	H = malloc((nu + 1) * sizeof *H);
+	ch = malloc((p.ncb + 1) * sizeof *ch);
+	cz = calloc(p.ncb + 1, sizeof *cz);
+	cd0 = calloc(p.ncb + 1, sizeof *cd0);
+	cstart = malloc((nb + 1) * sizeof *cstart);
+	if (!H || !ch || !cz || !cd0 || !cstart)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < nu; i++)
+		H[i] = u[i].h;
+	for (l = 0; l < p.ncb; l++)
+		ch[l] = p.cb[l].c_ptr;
+	c_by_last_batch(&p, H, bstart, nb, ch, cz, cd0, (size_t)p.ncb, cstart);
+	for (k = 0; k < nb; k++)
+		for (i = cstart[k]; i < cstart[k + 1]; i++)
+			if (xmg_hmap_put(&fin, ch[i], k))
+				xm_fatal("%s: out of memory", __func__);
 	xmg_hmap_init(&dmap);
 	for (k = 0; k < nb && st == XMG_OK; k++) {
 		xmg_hmap_free(&dmap);
@@ -1430,6 +1609,10 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 			if (cd->m != cs->m || cd->n != cs->n ||
 			    cd->c_ptr != cs->c_ptr || cd->eA != cs->eA ||
 			    cd->eB != cs->eB)
+				ok = 0;
+			/* no block of c goes back before a batch that feeds it */
+			if (cd->npairs > 0 && (!xmg_hmap_get(&fin, cs->c_ptr, &fv) ||
+			    fv < k))
 				ok = 0;
 			for (j = 0, q = 0; j < cd->npairs; j++, q++) {
 				const xmgd_pair_t *pd = &dp.pairs[cd->first_pair + j];
@@ -1472,7 +1655,9 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 		out[3] = ok;
 	}
 	xmg_hmap_free(&dmap);
+	xmg_hmap_free(&fin);
 done:
+	free(H); free(ch); free(cz); free(cd0); free(cstart);
 	free(off);
 	free(bstart);
 	free(used);
@@ -1507,6 +1692,8 @@ struct stream_plan {
 	uint64_t bulk;
 	size_t nr, ncw;
 	uint64_t *RH, *RSZ, *RD, *CH, *CSZ, *CD;
+	size_t *cstart;             /* C* final after batch k: cstart[k] ..
+	                               cstart[k + 1] - 1 */
 	xmg_hmap_t vmap;            /* a's and c's handles -> addresses */
 	/* a's split-precision operands, prepared by batch 0 for the later
 	 * batches (a_share 1): slices, exponent table, Inf/NaN flag in abuf */
@@ -1544,7 +1731,7 @@ sp_free(struct stream_plan *sp)
 	xmg_hmap_free(&sp->vmap);
 	free(sp->bstart); free(sp->H); free(sp->SZ); free(sp->D);
 	free(sp->RH); free(sp->RSZ); free(sp->RD);
-	free(sp->CH); free(sp->CSZ); free(sp->CD);
+	free(sp->CH); free(sp->CSZ); free(sp->CD); free(sp->cstart);
 	free(sp->bp); free(sp->bflops); free(sp->bnpairs);
 	free(sp);
 }
@@ -1656,6 +1843,8 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	}
 	for (i = 0; i < sp->nu; i++)
 		sp->total += u[i].sz;
+	if (stream_order_output())
+		order_by_output(p0, u, sp->nu);
 	/* within the budget a pagefile b is staged whole: one batch, still
 	 * read by the parallel readers; a host b is always streamed */
 	double first = 0, growth = 1;
@@ -1700,6 +1889,13 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		st = bulk_views(a, c, creal(beta) != 0 || cimag(beta) != 0,
 		    &sp->bulk, &sp->vmap, &sp->RH, &sp->RSZ, &sp->RD, &sp->nr,
 		    &sp->CH, &sp->CSZ, &sp->CD, &sp->ncw);
+	/* c's blocks by the batch after which they are final */
+	if (st == XMG_OK) {
+		if ((sp->cstart = malloc((sp->nb + 1) * sizeof *sp->cstart)) == NULL)
+			xm_fatal("%s: out of memory", __func__);
+		c_by_last_batch(p0, sp->H, sp->bstart, sp->nb, sp->CH, sp->CSZ,
+		    sp->CD, sp->ncw, sp->cstart);
+	}
 	if (st == XMG_OK)
 		st = xmgd_sync();
 	if (st != XMG_OK) {
@@ -1710,21 +1906,34 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	return XMG_OK;
 }
 
-/* Move c's staged blocks back: pagefile through the readers, host
- * blocks straight into their pinned memory. */
+/* A job moving c's staged blocks i0 .. i1 - 1 (of C*) back: pagefile
+ * through the readers, host blocks straight into their pinned memory. */
 static int
-sp_commit(struct stream_plan *sp, xm_tensor_t *c)
+c_write_start(struct stream_plan *sp, xm_tensor_t *c, size_t i0, size_t i1,
+    struct io_job *j)
 {
-	struct io_job j;
+	memset(j, 0, sizeof *j);
+	j->al = c->allocator;
+	j->h = sp->CH + i0; j->sz = sp->CSZ + i0; j->dst = sp->CD + i0;
+	j->n = i1 - i0; j->wr = 1;
+	j->merge = 1; j->seg = j->n;	/* c's views: one bulk buffer */
+	return j->n ? io_start(j) : XMG_OK;
+}
 
-	if (sp->ncw == 0)
-		return XMG_OK;
-	memset(&j, 0, sizeof j);
-	j.al = c->allocator;
-	j.h = sp->CH; j.sz = sp->CSZ; j.dst = sp->CD; j.n = sp->ncw; j.wr = 1;
-	j.merge = 1; j.seg = j.n;	/* c's views: one bulk buffer */
-	int st = io_start(&j);
-	return st == XMG_OK ? io_join(&j) : st;
+/*
+ * c's blocks go back batch by batch, each block once the batch holding its
+ * last pair has run, while the later batches run (XMG_STREAM_CWRITE=0
+ * writes all of c after the last batch).  Not with pagefile readers
+ * staging b: the write-back's readers would share their pinned slots.
+ */
+static int
+c_write_early(const struct stream_plan *sp)
+{
+	const char *e = getenv("XMG_STREAM_CWRITE");
+
+	if (e && strcmp(e, "0") == 0)
+		return 0;
+	return xmg_alloc_is_host(sp->b->allocator) || stage_mapped();
 }
 
 /*
@@ -1781,7 +1990,8 @@ static int
 sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 {
 	struct batch_buf bb = {NULL, NULL, NULL, NULL, NULL, NULL};
-	struct io_job io[2];
+	struct io_job io[2], cw;
+	const int early = c_write_early(sp);
 	uint64_t *JH = NULL, *JSZ = NULL, *JD = NULL, abytes = 0;
 	int64_t *offg = NULL, *offl = NULL;
 	xmg_hmap_t filt;
@@ -1794,6 +2004,7 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 	const int trace = tr && strcmp(tr, "0") != 0;
 
 	memset(io, 0, sizeof io);
+	memset(&cw, 0, sizeof cw);
 	memset(&acc, 0, sizeof acc);
 	acc.gemm_policy = -1;
 	xmg_hmap_init(&filt);
@@ -1916,6 +2127,15 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 			if (st == XMG_OK)
 				st = s2;
 		}
+		/* c's blocks final after batch k go back (one write-back job
+		 * at a time) */
+		if (st == XMG_OK && early &&
+		    sp->cstart[k + 1] > sp->cstart[k]) {
+			st = io_join(&cw);
+			if (st == XMG_OK)
+				st = c_write_start(sp, c, sp->cstart[k],
+				    sp->cstart[k + 1], &cw);
+		}
 		tw += now_ms() - t0;
 		if (trace) {
 			uint64_t bytes = 0;
@@ -1930,8 +2150,14 @@ sp_run(struct stream_plan *sp, const plan_t *p0, xm_tensor_t *c)
 	for (k = 0; k < 2; k++)
 		io_join(&io[k]);	/* never leave a copy in flight */
 	double tc = now_ms();
-	if (st == XMG_OK)
-		st = sp_commit(sp, c);
+	{
+		int s2 = io_join(&cw);
+		if (st == XMG_OK)
+			st = s2;
+	}
+	if (st == XMG_OK && !early && (st = c_write_start(sp, c, 0, sp->ncw,
+	    &cw)) == XMG_OK)
+		st = io_join(&cw);
 	if (trace)
 		fprintf(stderr, "xmg stream: c written back in %.2f ms\n",
 		    now_ms() - tc);

@@ -257,17 +257,21 @@ def test_gemm_work_lists_hold_their_invariants(engine, pagefile, name):
             t.free(data=True)
 
 
+@pytest.mark.parametrize("order", ["output", "file"])
 @pytest.mark.parametrize("name,nbatch", [("cfg2", 1), ("cfg2", 4), ("cfg2", 13),
                                          ("cfg3", 5), ("cfg5", 3)])
-def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbatch):
+def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbatch, order,
+                                                    monkeypatch):
     """The out-of-core path builds the whole plan once and cuts each batch's
     plan from it.  Cut on the host for b's blocks in nbatch runs, and in the
-    streamed path's own batches of at most a region's bytes: every merged
-    pair lands in exactly one batch, in its output block's order, with its
-    views and tables; the flops add up to the whole plan's; every batch's
-    stacked work list holds the kernel's invariants; every block lies
-    aligned inside its batch's region; a block larger than the region is
-    refused."""
+    streamed path's own batches of at most a region's bytes, with b's
+    blocks in the output blocks' order or in file order: every merged pair
+    lands in exactly one batch, in its output block's order, with its views
+    and tables; the flops add up to the whole plan's; every batch's stacked
+    work list holds the kernel's invariants; every block lies aligned
+    inside its batch's region; no block of c is written back before a batch
+    that feeds it; a block larger than the region is refused."""
+    monkeypatch.setenv("XMG_STREAM_ORDER", order)
     gen = {"cfg2": lambda: W.cfg2(engine, pagefile),
            "cfg3": lambda: W.cfg3(engine, pagefile, dtype=api.DOUBLE_COMPLEX),
            "cfg5": lambda: W.cfg5(engine, pagefile, v_blocks=8)}[name]
@@ -309,14 +313,16 @@ def test_out_of_core_batch_plans_partition_the_plan(engine, pagefile, name, nbat
 
 
 @pytest.mark.parametrize("ci", range(len(cases.CONTRACT_TESTS)))
-def test_plan_checks_on_reference_cases(engine, pagefile, ci):
+def test_plan_checks_on_reference_cases(engine, pagefile, ci, monkeypatch):
     """Every contraction case of the reference's test driver, all four
     scalar types: each work-list policy of the split-precision GEMM holds
     the kernel's invariants, and the out-of-core batch plans for b's blocks
-    in 1, 2 and 5 runs partition the whole plan."""
+    in 1, 2 and 5 runs partition the whole plan (b's blocks in the output
+    blocks' order for two of the types, in file order for the others)."""
     make, ia, ib, ic = cases.CONTRACT_TESTS[ci]
     out = (api.C.c_longlong * 4)()
     for dt in H.TYPES:
+        monkeypatch.setenv("XMG_STREAM_ORDER", "output" if dt % 2 == 0 else "file")
         a, b, c = make(engine, pagefile, dt)
         try:
             args = (a.h, b.h, c.h, ia.encode(), ib.encode(), ic.encode())
@@ -330,6 +336,33 @@ def test_plan_checks_on_reference_cases(engine, pagefile, ci):
         finally:
             for t in (a, b, c):
                 t.free()
+
+
+def _runs(engine, h, sz, dst):
+    n = len(h)
+    arr = lambda v: (api.C.c_uint64 * max(n, 1))(*v)
+    start = (api.C.c_size_t * max(n, 1))()
+    q = engine.xmg_copy_runs(arr(h), arr(sz), arr(dst), n, start)
+    return list(start[:q])
+
+
+def test_copy_runs(engine):
+    """The staging copies: one per run of blocks that follow one another
+    with only alignment padding between, in host memory and in HBM alike;
+    equal end-to-end distances alone never merge (two equal-sized blocks
+    that trade places between the two sides would be swapped)."""
+    # three blocks carved one after another on both sides (256-byte padding)
+    assert _runs(engine, [0, 256, 768], [200, 500, 10], [4096, 4352, 4864]) == [0]
+    # a block missing from the list between two listed ones: no merge
+    assert _runs(engine, [0, 512], [200, 200], [4096, 4608]) == [0, 1]
+    # equal-sized blocks in another order on the host side
+    # (host: x0 x2 x1, device: x0 x1 x2; list x0, x1): not one copy
+    assert _runs(engine, [0, 512], [200, 200], [4096, 4352]) == [0, 1]
+    assert _runs(engine, [0, 256, 512], [200, 200, 200], [4096, 4608, 4352]) == [0, 1, 2]
+    # a descending host address or a different distance: new runs
+    assert _runs(engine, [512, 0], [100, 100], [4096, 4352]) == [0, 1]
+    assert _runs(engine, [0, 256], [100, 100], [4096, 4608]) == [0, 1]
+    assert _runs(engine, [], [], []) == []
 
 
 def test_blocks_beyond_int32_offsets_are_refused(engine, pagefile):

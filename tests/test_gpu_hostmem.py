@@ -185,6 +185,29 @@ def test_shared_a_side(engine, oracle, hal, oal, monkeypatch):
     assert slice_bytes["1"] < slice_bytes["0"], slice_bytes
 
 
+@pytest.mark.parametrize("order,early", [("file", "1"), ("output", "0"), ("output", "1")])
+def test_stream_orders(engine, oracle, hal, oal, monkeypatch, order, early):
+    """b's batches cut in file order or in the output blocks' order
+    (XMG_STREAM_ORDER), c written back after the last batch or block by
+    block once final (XMG_STREAM_CWRITE): the oracle's result every way,
+    with beta accumulating over repeated calls of the kept plan."""
+    monkeypatch.setenv("XMG_STREAM_ORDER", order)
+    monkeypatch.setenv("XMG_STREAM_CWRITE", early)
+    we, wo = W.cfg2(engine, hal, scale=4), W.cfg2(oracle, oal, scale=4)
+    try:
+        for w in (we, wo):
+            W.fill(w.c, 41, W.LADDER_ANTISYM)
+            w.alpha, w.beta = -1.1, 0.5
+        for step in range(3):
+            we.run()
+            wo.run()
+            assert api.last_stats(engine).stage_batches > 1
+            assert W.rel_frobenius(W.read_canonical(we.c), W.read_canonical(wo.c)) <= REL, step
+    finally:
+        we.free()
+        wo.free()
+
+
 def test_elementwise_host_memory(engine, oracle, hal, oal):
     """xm_set, xm_add with a permutation, xm_dot on host-memory tensors."""
     for dt in (api.DOUBLE, api.FLOAT_COMPLEX):
