@@ -81,8 +81,7 @@ int xmg_work_list_check(const xm_tensor_t *a, const xm_tensor_t *b,
 
 /* The out-of-core batch plans, cut on the host without a device from the
  * whole plan, for b's blocks (in the streamed path's order: file order,
- * or the order of the output blocks they feed under
- * XMG_STREAM_ORDER=output) in the
+ * or the output blocks' with XMG_STREAM_ORDER=output) in the
  * streamed path's batches of at most `region` bytes, or, with region <= 0,
  * in nbatch equal runs: out = {batches, pairs over all batches, work-list
  * items of `policy` over all batches, 1 if every block lies aligned inside

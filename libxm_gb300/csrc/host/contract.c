@@ -1291,18 +1291,22 @@ form_batches(const struct hsz *u, size_t nu, size_t region, double first,
 	return XMG_OK;
 }
 
-/* XMG_STREAM_ORDER=output cuts b's batches in the output blocks' order
- * (order_by_output) instead of file order.  Not the default: where b's
- * contracted indices lead (the ladders' "cdab"), a batch in output order
- * is a block from every run of the file, its copies no longer merge, and
- * on a GB300 the host link moved such batches at ~147 GB/s against ~212
- * for merged ones, while the kernels ran no faster (cfg2 from host
- * memory: 53.8 ms per call against 52.3 in file order). */
+/* b's batches in the output blocks' order (order_by_output) with
+ * XMG_STREAM_ORDER=output, else in file order.  Where b's contracted
+ * indices lead (the ladders' "cdab"), a batch in output order takes a
+ * block from every run of the file: measured on a GB300, host-memory
+ * copies no longer merge and the link moved such batches at ~147 GB/s
+ * against ~212 for merged ones, with kernels no faster (cfg2 from host
+ * memory: 53.8 ms per call against 52.3), and copies from a pagefile's
+ * mapping ran 10-20 % slower, about what the early write-back of c won
+ * (cfg2 from a pagefile: 107-108 ms against 110-111; cfg5's structure
+ * with b = 60 GB: 1151-1266 ms against 1169-1217). */
 static int
-stream_order_output(void)
+stream_order_output(const xm_allocator_t *bal)
 {
 	const char *e = getenv("XMG_STREAM_ORDER");
 
+	(void)bal;
 	return e && strcmp(e, "output") == 0;
 }
 
@@ -1542,7 +1546,7 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 		return st;
 	}
 	nu = distinct_b(&p, &u);
-	if (stream_order_output())
+	if (stream_order_output(b->allocator))
 		order_by_output(&p, u, nu);
 	batch_buf_alloc(&bb, &p);
 	used = calloc(p.npr + 1, 1);
@@ -1843,7 +1847,7 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	}
 	for (i = 0; i < sp->nu; i++)
 		sp->total += u[i].sz;
-	if (stream_order_output())
+	if (stream_order_output(b->allocator))
 		order_by_output(p0, u, sp->nu);
 	/* within the budget a pagefile b is staged whole: one batch, still
 	 * read by the parallel readers; a host b is always streamed */
