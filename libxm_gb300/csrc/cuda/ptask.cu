@@ -21,14 +21,21 @@
  *    fit one tile; a CTA moves whole s0 x s1 slices through padded shared
  *    memory (loads along the source's runs, stores along the
  *    destination's): the gather-transpose of unfold/fold;
- *  - tile: the same for larger extents, TILE x TILE tiles.
+ *  - tile: the same for larger extents, TILE x TILE tiles;
+ *  - slab: xm_copy's transposes when each s0 x s1 slice lies contiguously
+ *    on both sides and consecutive slices follow one another (whole
+ *    blocks whose permutation swaps the two leading dimensions): a CTA
+ *    brings its slices in with one bulk copy into shared memory,
+ *    transposes there and stores along the destination's run.
  */
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <type_traits>
 #include <vector>
 
 #include "common.cuh"
+#include "tc.cuh"
 
 namespace xmg {
 
@@ -46,11 +53,16 @@ static inline int mt_host(int dbytes, int sbytes)
 	return sbytes <= 8 && dbytes <= 8 ? 48 : 32;
 }
 constexpr int MAT_MAXQ = 64;       /* slices per CTA at most */
+/* slab schedule: about SLAB_CHUNK bytes of slices per CTA (one slice at
+ * least), at most SLAB_SMEM bytes of shared memory (the source's slices
+ * and the padded tile) */
+constexpr int64_t SLAB_CHUNK = 16384;
+constexpr int64_t SLAB_SMEM = 64 * 1024;
 
 
 struct task_meta {
 	int64_t first_cta;
-	int32_t mode;          /* 0 row, 1 tile, 2 flat, 3 matrix */
+	int32_t mode;          /* 0 row, 1 tile, 2 flat, 3 matrix, 4 slab */
 	int32_t rows_per_cta;  /* row mode: outer rows per CTA */
 	int64_t nouter;        /* row: product of dims 1..; tile: dims 2.. */
 	int32_t ctas_d0, ctas_d1;
@@ -439,11 +451,155 @@ ptask_kernel(const xmgd_ptask_t *__restrict__ tasks,
 	}
 }
 
+/* a bounded wait of the slab schedule gave up (set on the device, read
+ * and cleared by the host after the launches) */
+__device__ int g_slab_err;
+
+/*
+ * Slab schedule: rows_per_cta consecutive s0 x s1 slices per CTA, each
+ * contiguous on both sides (source: dim 1 unit stride, dim 0 stride s1;
+ * destination: dim 0 unit stride, dim 1 stride s0; slice q at q * s0 * s1
+ * on both), 16-byte aligned.  One bulk copy brings the CTA's slices of the
+ * source into shared memory (one instruction, where the matrix schedule
+ * issues a copy per element); the source goes into a tile with an odd row
+ * pitch, so that both the transposing pass (threads along the source's
+ * run) and the storing pass (threads along the destination's run) touch
+ * distinct banks; stores follow the destination's run.
+ */
+template <typename T>
+__global__ void __launch_bounds__(PT_THREADS, 6)
+slab_kernel(const xmgd_ptask_t *__restrict__ tasks,
+    const task_meta *__restrict__ meta, int ntasks, int64_t cta0)
+{
+	extern __shared__ __align__(16) unsigned char dsm[];
+	__shared__ __align__(8) uint64_t bar;
+	__shared__ int s_err;
+
+	const int64_t cta = cta0 + blockIdx.x;
+	int lo = 0, hi = ntasks - 1;
+	while (lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if (meta[mid].first_cta <= cta) lo = mid; else hi = mid - 1;
+	}
+	const xmgd_ptask_t &t = tasks[lo];
+	const task_meta &m = meta[lo];
+	const int s0 = (int)t.size[0], s1 = (int)t.size[1], n = s0 * s1;
+	const int ld = s0 | 1;
+	const int64_t o0 = (cta - m.first_cta) * m.rows_per_cta;
+	const int k = (int)(m.nouter - o0 < m.rows_per_cta ? m.nouter - o0 :
+	    m.rows_per_cta);
+	const int kn = k * n;
+	const uint32_t cbytes = (uint32_t)kn * (uint32_t)sizeof(T);
+	const T *sb = reinterpret_cast<const T *>(dsm);
+	T *tb = reinterpret_cast<T *>(dsm + cbytes);
+	T *dst = reinterpret_cast<T *>(t.dst) + o0 * n;
+	const T *src = reinterpret_cast<const T *>(t.src) + o0 * n;
+	const T al = num<T>::mk(t.alpha);
+
+	const uint32_t b = smem_u32(&bar);
+	if (threadIdx.x == 0) {
+		s_err = 0;
+		mbar_init(b, 1);
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		mbar_expect_tx(b, cbytes);
+		bulk_g2s(smem_u32(dsm), src, cbytes, b);
+	}
+	const bool ok = mbar_wait(b, 0, &s_err, &g_slab_err, 1);
+	/* every thread leaves together when the wait gave up */
+	if (__syncthreads_or(!ok))
+		return;
+	/* source order e = q n + i0 s1 + i1 -> tile q s1 ld + i1 ld + i0 */
+	{
+		int q = threadIdx.x / n, r = threadIdx.x - q * n;
+		int i0 = r / s1, i1 = r - i0 * s1;
+		const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
+		const int d0 = dr / s1, d1 = dr - d0 * s1;
+		for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
+			tb[(q * s1 + i1) * ld + i0] = sb[e];
+			i1 += d1;
+			if (i1 >= s1) { i1 -= s1; i0++; }
+			i0 += d0;
+			if (i0 >= s0) { i0 -= s0; q++; }
+			q += dq;
+		}
+	}
+	__syncthreads();
+	/* destination order e = q n + i1 s0 + i0 */
+	int q = threadIdx.x / n, r = threadIdx.x - q * n;
+	int i1 = r / s0, i0 = r - i1 * s0;
+	const int dq = PT_THREADS / n, dr = PT_THREADS - dq * n;
+	const int d1 = dr / s0, d0 = dr - d1 * s0;
+	for (int e = threadIdx.x; e < kn; e += PT_THREADS) {
+		dst[e] = num<T>::mul(al, tb[(q * s1 + i1) * ld + i0]);
+		i0 += d0;
+		if (i0 >= s0) { i0 -= s0; i1++; }
+		i1 += d1;
+		if (i1 >= s1) { i1 -= s1; q++; }
+		q += dq;
+	}
+}
+
+/* the slab schedule for a task: slices per CTA (0 when the schedule does
+ * not apply: xm_copy of one scalar type only; an op that reads the
+ * destination ran slower with its second bulk copy, 0.69 of HBM against
+ * the matrix schedule's 0.71), and the CTA's shared memory */
+static int64_t
+slab_shape(const xmgd_ptask_t &t, int dbytes, int sbytes, int mt,
+    int64_t *smem)
+{
+	if (dbytes != sbytes || t.op != XMGD_OP_COPY || t.ndim < 2 || t.ndim > 3)
+		return 0;
+	const int64_t s0 = t.size[0], s1 = t.size[1], n = s0 * s1;
+	if (s0 > mt || s1 > mt || s0 < 2 || s1 < 2 ||
+	    t.dst_stride[0] != 1 || t.dst_stride[1] != s0 ||
+	    t.src_stride[1] != 1 || t.src_stride[0] != s1 ||
+	    (t.ndim == 3 && (t.dst_stride[2] != n || t.src_stride[2] != n)) ||
+	    (n * sbytes) % 16 != 0 || ((t.dst | t.src) & 15) != 0)
+		return 0;
+	int64_t k = n * sbytes >= SLAB_CHUNK ? 1 : SLAB_CHUNK / (n * sbytes);
+	const int64_t cap = t.ndim == 3 ? t.size[2] : 1;
+	if (k > cap)
+		k = cap;
+	*smem = k * n * sbytes + k * s1 * (s0 | 1) * sbytes;
+	return *smem <= SLAB_SMEM ? k : 0;
+}
+
+template <typename D, typename S>
+static int
+launch_slab(const xmgd_ptask_t *dtasks, const task_meta *dmeta, int ntasks,
+    int64_t cta0, int64_t n, int64_t smem)
+{
+	if constexpr (std::is_same<D, S>::value) {
+		static bool attr = false;
+		if (!attr) {
+			XMG_CK(cudaFuncSetAttribute(slab_kernel<D>,
+			    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SLAB_SMEM));
+			attr = true;
+		}
+		slab_kernel<D><<<(unsigned)n, PT_THREADS, (size_t)smem, stream()>>>(
+		    dtasks, dmeta, ntasks, cta0);
+		g_launches++;
+		XMG_CK(cudaGetLastError());
+		return XMG_OK;
+	} else {
+		return xmg_seterr(XMG_EINVAL, "slab schedule: scalar conversion");
+	}
+}
+
 template <typename D, typename S>
 static int
 launch(const xmgd_ptask_t *dtasks, const task_meta *dmeta, int ntasks,
-    const int64_t *begin, double *dpartial)
+    const int64_t *begin, int64_t slab_smem, double *dpartial)
 {
+	if (begin[5] > begin[4]) {
+		int st = launch_slab<D, S>(dtasks, dmeta, ntasks, begin[4],
+		    begin[5] - begin[4], slab_smem);
+		if (st)
+			return st;
+	}
 	/* one launch per schedule, over that schedule's CTA range */
 	for (int mode = 0; mode < 4; mode++) {
 		const int64_t n = begin[mode + 1] - begin[mode];
@@ -480,16 +636,32 @@ elem_bytes(int type)
 static void
 plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int dtype, int stype,
     std::vector<xmgd_ptask_t> &sorted, std::vector<task_meta> &meta,
-    std::vector<int> &order, int64_t begin[5])
+    std::vector<int> &order, int64_t begin[6], int64_t *slab_smem)
 {
 	std::vector<task_meta> m0((size_t)ntasks);
 	std::vector<int64_t> cnt((size_t)ntasks);
 	const int mt = mt_host(elem_bytes(dtype), elem_bytes(stype));
+	const char *e = getenv("XMG_PTASK_SLAB");
+	const bool slab_on = !(e && strcmp(e, "0") == 0);
 
+	/* the slab launch's shared memory: the largest of its CTAs' */
+	*slab_smem = 0;
 	for (int i = 0; i < ntasks; i++) {
 		const xmgd_ptask_t &t = tasks[i];
 		task_meta &m = m0[i];
 		memset(&m, 0, sizeof m);
+		int64_t need = 0;
+		const int64_t k = slab_on ? slab_shape(t, elem_bytes(dtype),
+		    elem_bytes(stype), mt, &need) : 0;
+		if (k > 0) {
+			m.mode = 4;
+			m.nouter = t.ndim == 3 ? t.size[2] : 1;
+			m.rows_per_cta = (int32_t)k;
+			m.ctas_d0 = 1;
+			cnt[i] = (m.nouter + k - 1) / k;
+			*slab_smem = std::max(*slab_smem, need);
+			continue;
+		}
 		const bool nosrc = t.op == XMGD_OP_SET || t.op == XMGD_OP_SCALE;
 		const bool tile = t.ndim >= 2 && t.src_stride[1] == 1 &&
 		    t.src_stride[0] != 1 && !nosrc;
@@ -540,7 +712,7 @@ plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int dtype, int stype,
 	meta.clear();
 	order.clear();
 	int64_t n = 0;
-	for (int mode = 0; mode < 4; mode++) {
+	for (int mode = 0; mode < 5; mode++) {
 		begin[mode] = n;
 		for (int i = 0; i < ntasks; i++)
 			if (m0[i].mode == mode) {
@@ -552,16 +724,16 @@ plan_tasks(const xmgd_ptask_t *tasks, int ntasks, int dtype, int stype,
 				order.push_back(i);
 			}
 	}
-	begin[4] = n;
+	begin[5] = n;
 }
 
 static int
 launch_types(int dtype, int stype, const xmgd_ptask_t *dt, const task_meta *dm,
-    int ntasks, const int64_t *begin, double *dp)
+    int ntasks, const int64_t *begin, int64_t slab_smem, double *dp)
 {
 	int st;
 
-#define L(D, S) st = launch<D, S>(dt, dm, ntasks, begin, dp)
+#define L(D, S) st = launch<D, S>(dt, dm, ntasks, begin, slab_smem, dp)
 	if (dtype == stype) {
 		switch (dtype) {
 		case 0: L(float, float); break;
@@ -603,7 +775,8 @@ xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, int stype,
 	if (ntasks <= 0)
 		return XMG_OK;
 	/* batches staged for replay carry one type on both sides */
-	plan_tasks(tasks, ntasks, stype, stype, sorted, meta, order, b->begin);
+	plan_tasks(tasks, ntasks, stype, stype, sorted, meta, order, b->begin,
+	    &b->slab_smem);
 	if ((st = xmgd_alloc(tb + meta.size() * sizeof(task_meta), &b->dbuf)))
 		return st;
 	b->ntasks = ntasks;
@@ -623,7 +796,7 @@ xmgd_ptask_launch(int dtype, int stype, const xmgd_ptask_batch_t *b)
 		return XMG_OK;
 	return launch_types(dtype, stype, (const xmgd_ptask_t *)b->dbuf,
 	    (const task_meta *)(b->dbuf + task_bytes(b->ntasks)), b->ntasks,
-	    b->begin, nullptr);
+	    b->begin, b->slab_smem, nullptr);
 }
 
 extern "C" int
@@ -633,15 +806,16 @@ xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
 	std::vector<xmgd_ptask_t> sorted;
 	std::vector<task_meta> meta;
 	std::vector<int> order;
-	int64_t begin[5], nctas;
+	int64_t begin[6], nctas, slab_smem;
 	uint64_t dbuf, dpart = 0;
 	size_t tb, mb;
 	int st;
 
 	if (ntasks <= 0)
 		return XMG_OK;
-	plan_tasks(tasks, ntasks, dtype, stype, sorted, meta, order, begin);
-	nctas = begin[4];
+	plan_tasks(tasks, ntasks, dtype, stype, sorted, meta, order, begin,
+	    &slab_smem);
+	nctas = begin[5];
 	tb = task_bytes(ntasks);
 	mb = (size_t)ntasks * sizeof(task_meta);
 	if ((st = xmgd_scratch(2, tb + mb, &dbuf)) != XMG_OK)
@@ -654,11 +828,22 @@ xmgd_ptasks(int dtype, int stype, const xmgd_ptask_t *tasks, int ntasks,
 	    &dpart)) != XMG_OK)
 		return st;
 	if ((st = launch_types(dtype, stype, (const xmgd_ptask_t *)dbuf,
-	    (const task_meta *)(dbuf + tb), ntasks, begin, (double *)dpart)))
+	    (const task_meta *)(dbuf + tb), ntasks, begin, slab_smem,
+	    (double *)dpart)))
 		return st;
 	/* the task buffers are reused by the next batch: wait here */
 	if ((st = check(cudaStreamSynchronize(stream()), "ptask_kernel")))
 		return st;
+	if (begin[5] > begin[4]) {
+		int err = 0;
+		XMG_CK(cudaMemcpyFromSymbol(&err, g_slab_err, sizeof err));
+		if (err) {
+			const int zero = 0;
+			XMG_CK(cudaMemcpyToSymbol(g_slab_err, &zero, sizeof zero));
+			return xmg_seterr(XMG_ETIMEOUT, "slab schedule: a bulk copy "
+			    "did not complete within the bounded wait");
+		}
+	}
 	if (dots) {
 		std::vector<double> h((size_t)nctas * 2);
 		if ((st = xmgd_d2h(h.data(), dpart, h.size() * sizeof(double))))

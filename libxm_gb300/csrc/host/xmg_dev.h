@@ -86,7 +86,9 @@ typedef struct {
 typedef struct {
 	uint64_t dbuf;               /* tasks + schedule metadata (xmgd_free) */
 	int ntasks;
-	int64_t begin[5];            /* CTA range of each schedule */
+	int64_t begin[6];            /* CTA range of each schedule */
+	int64_t slab_smem;           /* dynamic shared memory of the slab
+	                                schedule's launch */
 } xmgd_ptask_batch_t;
 int xmgd_ptask_stage(const xmgd_ptask_t *tasks, int ntasks, int stype,
     xmgd_ptask_batch_t *b);

@@ -88,6 +88,43 @@ def test_add_copy(engine, oracle, gal, oal, ci):
             _check(res[1], res[3], dt)
 
 
+def test_slab_transposes(engine, oracle, gal, oal, monkeypatch):
+    """Permutations that swap the two leading indices of whole blocks
+    (b's "cdab" -> "dcab"): xm_copy through the slab schedule (one bulk
+    copy per CTA, the transpose in shared memory) where each slice's bytes
+    are a multiple of 16, the matrix schedule elsewhere (odd slices here)
+    and for the other operations.  Same results as the oracle in every
+    scalar type, and bit for bit the matrix schedule's (XMG_PTASK_SLAB=0)
+    for xm_copy, xm_add, xm_mul and xm_div."""
+    o, v = [4, 6], [6, 8, 7, 10]
+    for dt in H.TYPES:
+        res = {}
+        for name, lib, al, slab in (("slab", engine, gal, "1"), ("matrix", engine, gal, "0"),
+                                    ("oracle", oracle, oal, "1")):
+            monkeypatch.setenv("XMG_PTASK_SLAB", slab)
+            w = W.ladder(lib, al, o, v, seed=5, dtype=dt)
+            b2 = w.b.structure()
+            W.fill(b2, 77, W.LADDER_ANTISYM)
+            out = []
+            api.copy(b2, 1.25, w.b, "cdab", "dcab")
+            out.append(H.canon(b2))
+            api.add(0.5, b2, -0.75, w.b, "cdab", "dcab")
+            out.append(H.canon(b2))
+            api.mul(b2, w.b, "cdab", "dcab")
+            out.append(H.canon(b2))
+            api.div(b2, w.b, "cdab", "dcab")
+            out.append(H.canon(b2))
+            res[name] = out
+            b2.free()
+            w.free()
+        for x, y, z in zip(res["slab"], res["matrix"], res["oracle"]):
+            assert x.keys() == y.keys() == z.keys()
+            for k in x:
+                np.testing.assert_array_equal(x[k], y[k])
+                np.testing.assert_allclose(x[k], z[k], rtol=1e-4 if dt < 2 else 1e-12,
+                                           atol=H.TOL[dt])
+
+
 @pytest.mark.parametrize("ci", range(len(cases.MUL_DIV_TESTS)))
 def test_mul_div(engine, oracle, gal, oal, ci):
     make, ia, ib = cases.MUL_DIV_TESTS[ci]
