@@ -256,8 +256,9 @@ def block_costs(w):
 # DRAM bytes (read + write) of one split-precision GEMM launch on the cfg2
 # ladder, from a single-pass ncu capture of that kernel on this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum, the stacked work list the
-# tuner keeps, 256-element chunks; the command is in the launch-list profile)
-GEMM_DRAM_BYTES = 84.16e9 + 1.18e9
+# tuner keeps, 256-element chunks, two K steps per pipeline stage; the
+# command is in the launch-list profile)
+GEMM_DRAM_BYTES = 77.56e9 + 0.93e9
 
 
 def timed_calls(eng, fn, reps=3, warm=5):
