@@ -76,8 +76,6 @@ static inline int xmg_is_complex(xm_scalar_type_t t)
 static inline void xmg_scalar_pack(xm_scalar_t s, double out[2])
 { out[0] = creal(s); out[1] = cimag(s); }
 
-#endif /* XMG_HOST_H */
-
 int xmg_alloc_io(xm_allocator_t *a, uint64_t h, void *mem, size_t bytes,
     int wr);
 int xmg_alloc_read_range(xm_allocator_t *a, uint64_t h, size_t byte_off,
@@ -104,3 +102,5 @@ int xmg_ptask_run(xmg_ptask_list_t *l, int dtype, int stype, double *dots);
 void xmg_ptask_list_free(xmg_ptask_list_t *l);
 /* Strides (elements) of a canonical block of the given dims. */
 void xmg_canon_strides(const xm_dim_t *dims, int64_t strides[XM_MAX_DIM]);
+
+#endif /* XMG_HOST_H */
