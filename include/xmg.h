@@ -259,9 +259,12 @@ void xmg_host_free(void *p);
  * batch of b is copied on a side stream while the previous batch is
  * contracted, and c is copied back before the call returns (block by
  * block once final, as for the pagefile).  The batches
- * (about XMG_HOST_BATCHES of them, default 6, at most the staging region
- * each) grow by a factor XMG_HOST_GROWTH (default 1.15) from one to the
- * next, so that the first copy, which nothing overlaps, is short.  The
+ * (about XMG_HOST_BATCHES of them, default 8, at most the staging region
+ * each) grow by a factor XMG_HOST_GROWTH (default 1.45) from one to the
+ * next up to the middle and shrink again toward the end
+ * (XMG_HOST_SHAPE=geometric: grow to the end), so that the first copy,
+ * which nothing overlaps, and the last batch's kernels, which nothing
+ * overlaps where the host link is the slower side, are short.  The
  * streamed plan of the last such contraction (batches, HBM regions, the
  * device plans and their graphs) is kept while the tensors' block
  * structures and the call's arguments stay the same (XMG_STREAM_CACHE=0

@@ -537,15 +537,18 @@ distinct_b(const plan_t *p, struct hsz **out)
  * STAGE_ALIGN-aligned offset of its batch: batch k holds blocks bstart[k]
  * .. bstart[k + 1] - 1 (bstart[nb] = nu), block i at offset off[i];
  * *rbytes is the largest batch.  Batch k takes at most cap_k bytes, with
- * cap_k = region when first <= 0, else min(region, first * growth^k); a
- * block larger than cap_k (but within the region) makes a batch of its
- * own.  A block larger than the region is an error. */
+ * cap_k = region when first <= 0, else min(region, first * growth^e):
+ * e = k, or with tent = n > 0, e = min(k, n - 1 - k) (at least 0), so that
+ * the batches grow and then shrink again.  A block larger than cap_k (but
+ * within the region) makes a batch of its own.  A block larger than the
+ * region is an error. */
 static int
 form_batches(const struct hsz *u, size_t nu, size_t region, double first,
-    double growth, uint64_t *off, size_t *bstart, size_t *nb, uint64_t *rbytes)
+    double growth, int tent, uint64_t *off, size_t *bstart, size_t *nb,
+    uint64_t *rbytes)
 {
 	uint64_t run = 0;
-	double cap = first > 0 && first < (double)region ? first : (double)region;
+	double cap = (double)region;
 	size_t i;
 
 	*nb = 0;
@@ -557,8 +560,14 @@ form_batches(const struct hsz *u, size_t nu, size_t region, double first,
 			    "(%llu bytes) exceeds the staging region (%zu bytes)",
 			    (unsigned long long)u[i].sz, region);
 		if (i == 0 || (run > 0 && (double)(run + al) > cap)) {
-			if (i > 0 && first > 0) {
-				cap *= growth;
+			if (first > 0) {
+				long e = (long)*nb;
+				if (tent > 0) {
+					e = tent - 1 - e < e ? tent - 1 - e : e;
+					if (e < 0)
+						e = 0;
+				}
+				cap = first * pow(growth, (double)e);
 				if (cap > (double)region)
 					cap = (double)region;
 			}
@@ -841,7 +850,7 @@ xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 	if (region > 0) {
 		/* the streamed path's batches of at most `region` bytes: each
 		 * block inside the region, aligned, after the previous one */
-		if ((st = form_batches(u, nu, (size_t)region, 0, 1, off, bstart,
+		if ((st = form_batches(u, nu, (size_t)region, 0, 1, 0, off, bstart,
 		    &nb, &rbytes)) != XMG_OK)
 			goto done;
 		if (nu > 0 && (bstart[0] != 0 || bstart[nb] != nu ||
@@ -1044,27 +1053,38 @@ sp_match(const struct stream_plan *sp, xm_scalar_t alpha,
 	    strcmp(sp->idx[2], idxc) == 0;
 }
 
-/* host-allocator b: about XMG_HOST_BATCHES (default 6) batches growing
- * geometrically by XMG_HOST_GROWTH (default 1.15) per batch: the small
- * first batch is the only copy nothing overlaps, and a batch's kernels
- * (for the FP64 ladders about 5-6 ms per GB of b) outlast the copy of the
- * next one (4.7 ms per GB over a 212 GB/s link) while the growth stays
- * below their ratio (cfg2 ladder, measured: 6 batches at 1.15 57.4 ms per
- * call, 8 at 1.2 58.3, 8 at 1.0 60.3, 4 at 1.0 60.7, 2 at 1.0 67.4).
- * Returns the first batch's byte budget. */
+/* host-allocator b: about XMG_HOST_BATCHES (default 8) batches that
+ * grow by a factor XMG_HOST_GROWTH (default 1.45) per batch up to the
+ * middle and shrink again toward the end (XMG_HOST_SHAPE=tent, the
+ * default; =geometric keeps growing).  The small first batch is the only
+ * copy nothing overlaps; the small last one is the only kernels nothing
+ * overlaps where the host link is slower than the kernels consume b (a
+ * batch's kernels take about 5.5-6.5 ms per GB of b for the FP64 ladders,
+ * its copy 4.7 ms per GB at 212 GB/s, 7-8 ms at the 130-150 GB/s seen on
+ * some boxes, where the geometric schedule's last 1.6 GB batch left ~10 ms
+ * of kernels after the last copy).  Measured, cfg2 from host memory on a
+ * box with a 212 GB/s link (compute-bound): tent 8 at 1.45 51.7 ms per
+ * call, 8 at 1.3 52.2, 6 at 1.3 52.2, 8 at 1.2 52.6, 10 at 1.25 52.9;
+ * geometric 6 at 1.15 52.1.  Returns the first batch's byte budget;
+ * *tent is the batch count of the tent shape, 0 for geometric. */
 static double
-host_first_batch(uint64_t total, double *growth)
+host_first_batch(uint64_t total, double *growth, int *tent)
 {
 	const char *e = getenv("XMG_HOST_BATCHES"), *g = getenv("XMG_HOST_GROWTH");
-	double n = e ? atof(e) : 6, r = g ? atof(g) : 1.15;
+	const char *sh = getenv("XMG_HOST_SHAPE");
+	const int geo = sh && strcmp(sh, "geometric") == 0;
+	int n = e ? atoi(e) : 8, k;
+	double r = g ? atof(g) : 1.45, w = 0;
 
 	if (n < 1)
 		n = 1;
 	if (!(r >= 1.0))
 		r = 1.0;
 	*growth = r;
-	return r > 1.0 ? (double)total * (r - 1) / (pow(r, n) - 1) :
-	    (double)total / n;
+	*tent = geo ? 0 : n;
+	for (k = 0; k < n; k++)
+		w += pow(r, geo ? k : (k < n - 1 - k ? k : n - 1 - k));
+	return (double)total / w;
 }
 
 /* pagefile b beyond the staging budget: about XMG_STAGE_BATCHES (default
@@ -1142,8 +1162,9 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 	/* within the budget a pagefile b is staged whole: one batch, still
 	 * read by the parallel readers; a host b is always streamed */
 	double first = 0, growth = 1;
+	int tent = 0;
 	if (xmg_alloc_is_host(b->allocator))
-		first = host_first_batch(sp->total, &growth);
+		first = host_first_batch(sp->total, &growth, &tent);
 	else if (sp->total <= budget)
 		region = sp->total + sp->nu * STAGE_ALIGN;
 	else
@@ -1159,7 +1180,7 @@ sp_build(xm_scalar_t alpha, const xm_tensor_t *a, const xm_tensor_t *b,
 		sp->H[i] = u[i].h;
 		sp->SZ[i] = u[i].sz;
 	}
-	st = form_batches(u, sp->nu, region, first, growth, OFF, sp->bstart,
+	st = form_batches(u, sp->nu, region, first, growth, tent, OFF, sp->bstart,
 	    &sp->nb, &sp->rbytes);
 	free(u);
 	if (st == XMG_OK) {
