@@ -14,7 +14,7 @@ _LIB = None
 
 
 def build(verbose=False):
-    from .build import build as _build
+    from .builder import build as _build
     return _build(verbose=verbose)
 
 
