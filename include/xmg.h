@@ -102,6 +102,16 @@ int xmg_batch_plan_check(const xm_tensor_t *a, const xm_tensor_t *b,
 size_t xmg_copy_runs(const uint64_t *h, const uint64_t *sz,
     const uint64_t *dst, size_t n, size_t *start);
 
+/* The batches the streamed path cuts for b's distinct blocks of sizes
+ * sz[0 .. n - 1], in that order: for a host-memory b (host != 0, the
+ * XMG_HOST_* schedule) or a pagefile b beyond the staging budget
+ * (XMG_STAGE_BATCHES equal batches), each at most `region` bytes with its
+ * blocks 256-byte aligned; batch k holds blocks bstart[k] .. bstart[k + 1]
+ * - 1 (bstart holds n + 1 entries).  Returns the number of batches, 0
+ * when a block exceeds the region.  For tests. */
+size_t xmg_stream_batches(const uint64_t *sz, size_t n, size_t region,
+    int host, size_t *bstart);
+
 /* Statistics of the last xm_contract / xmg_contract on this process. */
 typedef struct {
 	double flops;            /* useful flops (see xmg_contract_flops) */

@@ -131,6 +131,8 @@ _GB_SIGS = {
     "xmg_copy_runs": (C.c_size_t, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64), C.c_size_t,
                                    C.POINTER(C.c_size_t)]),
+    "xmg_stream_batches": (C.c_size_t, [C.POINTER(C.c_uint64), C.c_size_t, C.c_size_t,
+                                        C.c_int, C.POINTER(C.c_size_t)]),
     "xmg_get_last_stats": (C.c_int, [C.POINTER(Stats)]),
     "xmg_synchronize": (C.c_int, []),
     "xmg_plan_cache_clear": (None, []),

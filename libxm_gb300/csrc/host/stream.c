@@ -1104,6 +1104,42 @@ file_batch(uint64_t total)
 	return (double)total / n;
 }
 
+/* the batches the streamed path cuts for b's distinct blocks of sizes
+ * sz[0 .. n - 1] (in that order): host-memory b (host != 0) or a pagefile
+ * b beyond the staging budget, batches of at most `region` bytes; batch k
+ * is blocks bstart[k] .. bstart[k + 1] - 1 (bstart holds n + 1 entries).
+ * Returns the number of batches, 0 on error.  For tests. */
+size_t
+xmg_stream_batches(const uint64_t *sz, size_t n, size_t region, int host,
+    size_t *bstart)
+{
+	struct hsz *u;
+	uint64_t *off, rbytes, total = 0;
+	double first, growth = 1;
+	size_t i, nb = 0;
+	int tent = 0;
+
+	if (n == 0)
+		return 0;
+	u = malloc(n * sizeof *u);
+	off = malloc(n * sizeof *off);
+	if (!u || !off)
+		xm_fatal("%s: out of memory", __func__);
+	for (i = 0; i < n; i++) {
+		u[i].h = i + 1;
+		u[i].sz = sz[i];
+		u[i].key = 0;
+		total += sz[i];
+	}
+	first = host ? host_first_batch(total, &growth, &tent) : file_batch(total);
+	if (form_batches(u, n, region, first, growth, tent, off, bstart, &nb,
+	    &rbytes) != XMG_OK)
+		nb = 0;
+	free(u);
+	free(off);
+	return nb;
+}
+
 /*
  * The batches, regions and staged views of a streamed contraction (no
  * device plans yet).  Returns XMG_OK with *sp set, or a status; *incore

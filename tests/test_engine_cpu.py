@@ -365,6 +365,61 @@ def test_copy_runs(engine):
     assert _runs(engine, [], [], []) == []
 
 
+def _stream_batches(engine, sizes, region, host):
+    n = len(sizes)
+    arr = (api.C.c_uint64 * n)(*sizes)
+    bstart = (api.C.c_size_t * (n + 1))()
+    nb = engine.xmg_stream_batches(arr, n, int(region), host, bstart)
+    return [list(range(bstart[k], bstart[k + 1])) for k in range(nb)]
+
+
+def test_stream_batch_schedules(engine, monkeypatch):
+    """The streamed path's batches of b: a partition of the blocks in
+    order, every batch within the region (256-byte aligned blocks); for a
+    host-memory b the default tent (sizes grow by XMG_HOST_GROWTH to the
+    middle and shrink again, so the first and the last batch are small),
+    the geometric shape on request; for a pagefile b about
+    XMG_STAGE_BATCHES equal batches; a block beyond the region refused."""
+    for k in ("XMG_HOST_SHAPE", "XMG_HOST_BATCHES", "XMG_HOST_GROWTH", "XMG_STAGE_BATCHES"):
+        monkeypatch.delenv(k, raising=False)
+    rng = np.random.default_rng(3)
+    sizes = [int(x) for x in rng.integers(1 << 20, 8 << 20, 1500)]
+    al = [(x + 255) // 256 * 256 for x in sizes]
+
+    def check(b, region):
+        assert [i for bb in b for i in bb] == list(range(len(sizes)))
+        assert all(sum(al[i] for i in bb) <= region for bb in b)
+        return [sum(sizes[i] for i in bb) for bb in b]
+
+    big = 32e9
+    got = check(_stream_batches(engine, sizes, big, 1), big)
+    assert 8 <= len(got) <= 9
+    planned = got[:8]
+    mid = max(planned)
+    assert mid > 2.5 * planned[0] and mid > 2.5 * planned[7], got
+    assert abs(planned[0] - planned[7]) < 0.3 * planned[0], got
+    assert planned.index(mid) in (3, 4)
+
+    monkeypatch.setenv("XMG_HOST_SHAPE", "geometric")
+    monkeypatch.setenv("XMG_HOST_BATCHES", "6")
+    monkeypatch.setenv("XMG_HOST_GROWTH", "1.15")
+    got = check(_stream_batches(engine, sizes, big, 1), big)
+    assert 6 <= len(got) <= 7
+    assert all(got[k + 1] > got[k] for k in range(5)), got
+
+    monkeypatch.setenv("XMG_STAGE_BATCHES", "5")
+    got = check(_stream_batches(engine, sizes, big, 0), big)
+    assert 5 <= len(got) <= 6
+    assert max(got[:5]) < 1.1 * min(got[:5]), got
+
+    # a region below the planned batches caps every batch
+    region = 200 << 20
+    got = check(_stream_batches(engine, sizes, region, 1), region)
+    assert len(got) > 30
+    # a block larger than the region
+    assert _stream_batches(engine, sizes, 4 << 20, 1) == []
+
+
 def test_blocks_beyond_int32_offsets_are_refused(engine, pagefile):
     """Offsets inside a block are 32-bit on the device: the planner refuses
     a block with more than 2^31 - 1 elements with an error instead of
