@@ -16,20 +16,22 @@
 /* out-of-core contraction                                             */
 
 /*
- * b's pagefile blocks are streamed through two HBM regions: reader threads
- * (XMG_STAGE_THREADS, default 12) read batch i+1 from the pagefile into
- * pinned 64 MiB chunks, two per reader used in turn, and copy each on the
- * side stream (cudaMemcpyAsync) into the idle region while batch i is
- * contracted on the compute stream.  Each batch is an
- * ordinary contraction restricted to the merged pairs whose b data lies in
- * the batch (pairs merge only over equal b data, so the restriction
- * commutes with merging); beta is applied by the first batch and the later
- * ones accumulate with beta = 1.  The plan is built once per call, with data
- * handles for addresses, and each batch's plan cut from it.  a's and c's
- * canonical blocks are staged whole, as views in one HBM buffer, by the same
- * readers together with batch 0 while batch 0's plan is cut; c is written
- * back by them in reverse (side-stream fetches into the pinned chunks,
- * pwrite).
+ * b's blocks are streamed through two HBM regions: batch i + 1 is copied on
+ * the side stream (cudaMemcpyAsync) into the idle region while batch i is
+ * contracted on the compute stream.  The copies come straight from the
+ * blocks' page-locked memory (host allocator), from a read-only mapping of
+ * the pagefile where the GPU reads pageable memory through the host's page
+ * tables, or else through reader threads (XMG_STAGE_THREADS, default 12)
+ * that read the pagefile into pinned 64 MiB chunks, two per reader used in
+ * turn.  Each batch is an ordinary contraction restricted to the merged
+ * pairs whose b data lies in the batch (pairs merge only over equal b
+ * data, so the restriction commutes with merging); beta is applied by the
+ * first batch and the later ones accumulate with beta = 1.  The plan is
+ * built once, with data handles for addresses, and each batch's plan cut
+ * from it; the batch plans are kept for repeated calls.  a's and c's
+ * canonical blocks are staged whole, as views in one HBM buffer, together
+ * with batch 0 while batch 0's plan is cut; c's blocks go back once final
+ * (pagefile: side-stream fetches into the readers' pinned chunks, pwrite).
  */
 #define STAGE_CHUNK ((size_t)64 << 20)
 #define STAGE_ALIGN 256
