@@ -16,7 +16,8 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
-    """CPU restatement of the reference algorithm (the checker)."""
+    """CPU restatement of the reference algorithm (the oracle the GPU results
+    are compared against)."""
     import oracle.build as ob
     from libxm_gb300 import api
     lib = api.Lib(ob.build_oracle())
